@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Benchmark: 512^3 all-triangle bispectra per second on GB300.
+
+Workload (one "step" = one full bispectrum of one mesh):
+  512^3 float32 lognormal mesh, L = 1000 Mpc/h, shells of width 2 k_f from
+  k_f to k_Nyq/2 (63 shells), all 24 305 auto triangle bins; the step runs
+  r2c of the mesh -> shell filter + batched c2r of 63 shells -> bf16 split ->
+  tcgen05 bf16x3 triple-product contraction -> FP64 normalisation by the
+  cached triangle counts.  Grid information (N_tri, k_mean) depends only on
+  the binning and is computed once before timing ("warm"); its one-off cost is
+  reported under "cold".
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N > 1) every rank measures its own meshes (replicas, no
+collective on the data path); the time is the max over ranks.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "512³ all-tri bispectra/s, bf16x3 vs FP32 at ≤1e-5 rel err; serve p50/p99 ms"
+NMESH, BOX = 512, 1000.0
+WORKLOAD = ("512^3 all-triangle auto bispectrum: L=1000 Mpc/h, 63 shells dk=2kf from kf to "
+            "kNyq/2, 24305 bins, lognormal float32 mesh (seed 1+rank), grid info cached")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="bf16x3")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true")
+    return ap.parse_args()
+
+
+def workload_bins():
+    from bskit_gb300 import bins
+    kf = 2 * math.pi / BOX
+    kw = dict(kmin=kf, kmax=(NMESH // 4) * kf, dk=2 * kf)
+    return bins.generate_bin_edge_list(**kw), bins.generate_triangle_bin_list(return_indices=True,
+                                                                              **kw)
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, \
+            "fallback"
+
+
+class ClockSampler(object):
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def kernel_launches_per_step(plan, precision):
+    """Kernels of libbskit_gb300 launched by one step (cuFFT's own kernels excluded)."""
+    chunks = (plan.n_shells + 7) // 8
+    n = 1 + chunks  # extract + filter chunks
+    if precision in ("bf16x3", "bf16"):
+        n += 1  # split
+    n += 1 + 1 + 1  # contraction + scale + normalize
+    return n
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from bskit_gb300 import synthetic
+    from bskit_gb300.engine import Plan
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    edges, tri = workload_bins()
+    plan = Plan(NMESH, BOX, edges, grid="reduced", device=dev)
+    ts = plan.triangles(tri)
+    delta = synthetic.lognormal_mesh_torch(NMESH, BOX, seed=1 + rank, device=dev).contiguous()
+    torch.cuda.synchronize()
+
+    # ---- cold: grid information (FP64), once
+    t0 = time.perf_counter()
+    ntri, kmean = plan.gridinfo(ts)
+    plan.sync_check()
+    cold_gridinfo_s = time.perf_counter() - t0
+
+    stream = torch.cuda.current_stream()
+    prec = args.precision
+
+    def step(p=prec):
+        plan.paint(0, delta)
+        b = plan.measure_b(ts, precision=p)
+        return plan.normalize(b, ntri)
+
+    def timed(fn, k, w):
+        for _ in range(w):
+            fn()
+        plan.sync_check()
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if dist is not None:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, out
+
+    clocks = ClockSampler(dev.index)
+    for _ in range(args.warmup):
+        step()
+    plan.sync_check()
+    clocks.start()
+    ms, bn = timed(step, args.steps, 0)
+    clk = clocks.stop()
+    plan.sync_check()
+    ms_step = ms / args.steps
+    value = world * args.steps / (ms / 1e3)
+
+    # ---- end to end through the public API: pinned host mesh in, B to host each step
+    host = delta.cpu().pin_memory()
+    dmesh = torch.empty_like(delta)
+    out_host = torch.empty(len(tri), dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        dmesh.copy_(host, non_blocking=True)
+        plan.paint(0, dmesh)
+        b = plan.measure_b(ts, precision=prec)
+        out_host.copy_(plan.normalize(b, ntri), non_blocking=True)
+        return out_host
+
+    e2e_ms, _ = timed(e2e_step, args.steps, 1)
+    e2e_value = world * args.steps / (e2e_ms / 1e3)
+
+    # ---- contraction alone (fields and split cached): the dominant kernel
+    plan.paint(0, delta)
+    step()
+    torch.cuda.synchronize()
+    reps = 5
+    c_ms, b_tc = timed(lambda: plan.measure_b(ts, precision=prec), reps, 1)
+    c_ms /= reps
+    ng = plan.ngrid
+    algo_flops = 2.0 * len(tri) * float(ng) ** 3
+    sched_cols = None
+    peaks, peak_kind = measured_peaks()
+    peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
+    achieved = algo_flops / (c_ms / 1e3) / 1e12
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "contract_tc_traffic.json")) as f:
+            tr = json.load(f)
+        traffic = tr.get("bytes_per_launch_512")
+    except Exception:
+        pass
+
+    # ---- plain FP32 path on the same workload, and agreement with it
+    fp32 = None
+    if not args.no_fp32:
+        k32 = max(1, min(args.steps, 3))
+        ms32, b32 = timed(lambda: step("fp32"), k32, 1)
+        bref = b32.double().cpu().numpy()
+        bt = bn.double().cpu().numpy()
+        rel = np.abs(bt - bref) / np.abs(bref)
+        fp32 = {"value": world * k32 / (ms32 / 1e3), "ms_per_step": ms32 / k32,
+                "bf16x3_vs_fp32_rel_err": {"max": float(np.nanmax(rel)),
+                                           "median": float(np.nanmedian(rel)),
+                                           "p99": float(np.nanpercentile(rel, 99))}}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle.cpu_baseline import ReferenceCPU
+        ref = ReferenceCPU(delta.cpu().numpy(), BOX, edges, tri)
+        try:
+            est = ref.step()
+            cpu = {"value": 1.0 / est, "unit": "bispectra/s", "cores": ref.P, "kind": "port",
+                   "sample": ref.describe(), "sample_seconds": ref.last["sample_seconds"]}
+        finally:
+            ref.close()
+
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "bispectra/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": prec,
+        "data": "synthetic lognormal mesh (seeded), no dataset",
+        "config": {"workload": WORKLOAD, "nmesh": NMESH, "box": BOX, "n_shells": len(edges),
+                   "n_bins": int(len(tri)), "precision": prec, "contraction_grid": ng,
+                   "l2": "inputs larger than L2 (mesh 512 MiB, shell fields %.1f GiB)"
+                         % (len(edges) * ng ** 3 * 4 / 2 ** 30),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e_value, "unit": "bispectra/s",
+                "h2d_bytes_per_step": int(host.numel() * 4),
+                "d2h_bytes_per_step": int(out_host.numel() * 8),
+                "ms_per_step": e2e_ms / args.steps},
+        "gpu_launches": kernel_launches_per_step(plan, prec) * args.steps,
+        "roofline": {"kernel": "contract_tc_kernel (tcgen05 bf16x3)", "bound": "tensor",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "%s bf16_tflops_sustained" % peak_kind,
+                     "algorithmic_flops_per_launch": algo_flops,
+                     "launch_ms": c_ms},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "cold": {"gridinfo_s": cold_gridinfo_s},
+        "fp32_plain": fp32,
+    }
+    if fp32:
+        line["speedup_vs_fp32_plain"] = value / fp32["value"]
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+
+    from bskit_gb300 import synthetic
+    from oracle.cpu_baseline import ReferenceCPU
+
+    edges, tri = workload_bins()
+    delta = synthetic.lognormal_mesh(NMESH, BOX, seed=1)
+    ref = ReferenceCPU(delta, BOX, edges, tri)
+    try:
+        for _ in range(args.warmup):
+            ref.step()
+        t0 = time.perf_counter()
+        ests = [ref.step() for _ in range(args.steps)]
+        wall = time.perf_counter() - t0
+        est = float(np.mean(ests))
+        value = 1.0 / est
+        line = {
+            "impl": "reference", "metric": METRIC, "value": value, "unit": "bispectra/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": est * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic lognormal mesh (seeded)",
+            "config": {"workload": WORKLOAD, "nmesh": NMESH, "n_shells": len(edges),
+                       "n_bins": int(len(tri)), "parallelism": "%d host processes" % ref.P},
+            "cpu_baseline": {"value": value, "unit": "bispectra/s", "cores": ref.P,
+                             "kind": "port", "sample": ref.describe()},
+            "e2e": {"value": value, "unit": "bispectra/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "sample_wall_s": wall,
+        }
+        print(json.dumps(line))
+    finally:
+        ref.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

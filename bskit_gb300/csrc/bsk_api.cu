@@ -1,0 +1,575 @@
+// C ABI of the GB300 bispectrum engine: plans, cuFFT orchestration, dispatch.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+
+#include "bsk_internal.cuh"
+
+namespace bsk {
+
+namespace {
+thread_local std::string g_err;
+
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev_);
+    if (prev_ != dev) cudaSetDevice(dev);
+    dev_ = dev;
+  }
+  ~DeviceGuard() {
+    if (prev_ != dev_) cudaSetDevice(prev_);
+  }
+
+ private:
+  int prev_ = 0, dev_ = 0;
+};
+
+template <typename F>
+int guarded(F&& f) {
+  try {
+    f();
+    return BSK_OK;
+  } catch (const Error& e) {
+    g_err = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_err = "host allocation failed";
+    return BSK_ERR_OOM;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return BSK_ERR_ARG;
+  }
+}
+
+bool nice_size(int m) {
+  for (int p : {2, 3, 5, 7})
+    while (m % p == 0) m /= p;
+  return m == 1;
+}
+
+// Smallest even FFT-friendly Ng with Ng > 3*qmax (so no triple of shell modes
+// can alias onto k = 0) and Ng <= N; N itself when none exists.
+int choose_grid(int N, int qmax, int mode) {
+  if (mode == BSK_GRID_NATIVE) return N;
+  for (int m = 3 * qmax + 1; m < N; ++m)
+    if (m % 2 == 0 && nice_size(m) && m > 2 * qmax + 1) return m;
+  return N;
+}
+
+void* dmalloc(size_t bytes) {
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error{BSK_ERR_OOM, "cudaMalloc(" + std::to_string(bytes) + ") failed: " +
+                                 cudaGetErrorString(e)};
+  }
+  return p;
+}
+
+void* dmalloc_async(size_t bytes, cudaStream_t st) {
+  void* p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, bytes, st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error{BSK_ERR_OOM, "cudaMallocAsync(" + std::to_string(bytes) + ") failed: " +
+                                 cudaGetErrorString(e)};
+  }
+  return p;
+}
+
+void grow_work(bsk_plan* p, size_t ws) {
+  if (ws <= p->work_bytes) return;
+  if (p->work) cudaFree(p->work);
+  p->work = nullptr;
+  p->work = dmalloc(ws);
+  p->work_bytes = ws;
+}
+
+void make_c2r(bsk_plan* p) {
+  int n[3] = {p->Ng, p->Ng, p->Ng};
+  BSK_CHECK_CUFFT(cufftCreate(&p->c2r));
+  p->c2r_ok = true;
+  BSK_CHECK_CUFFT(cufftSetAutoAllocation(p->c2r, 0));
+  size_t ws = 0;
+  BSK_CHECK_CUFFT(cufftMakePlanMany(p->c2r, 3, n, nullptr, 1, (int)p->Mh, nullptr, 1,
+                                    (int)p->K, CUFFT_C2R, p->chunk, &ws));
+  grow_work(p, ws);
+}
+
+void make_z2d(bsk_plan* p) {
+  if (p->z2d_ok) return;
+  int n[3] = {p->Ng, p->Ng, p->Ng};
+  BSK_CHECK_CUFFT(cufftCreate(&p->z2d));
+  p->z2d_ok = true;
+  BSK_CHECK_CUFFT(cufftSetAutoAllocation(p->z2d, 0));
+  size_t ws = 0;
+  BSK_CHECK_CUFFT(cufftMakePlanMany(p->z2d, 3, n, nullptr, 1, (int)p->Mh, nullptr, 1,
+                                    (int)p->K, CUFFT_Z2D, p->chunk, &ws));
+  grow_work(p, ws);
+}
+
+void make_r2c(bsk_plan* p) {
+  BSK_CHECK_CUFFT(cufftCreate(&p->r2c));
+  p->r2c_ok = true;
+  BSK_CHECK_CUFFT(cufftSetAutoAllocation(p->r2c, 0));
+  size_t ws = 0;
+  BSK_CHECK_CUFFT(cufftMakePlan3d(p->r2c, p->N, p->N, p->N, CUFFT_R2C, &ws));
+  grow_work(p, ws);
+}
+
+void bind_work(bsk_plan* p, cufftHandle h, cudaStream_t st) {
+  BSK_CHECK_CUFFT(cufftSetWorkArea(h, p->work));
+  BSK_CHECK_CUFFT(cufftSetStream(h, st));
+}
+
+// Masked shell fields of `slot` for every shell: filter kernel + batched C2R.
+void ensure_fields(bsk_plan* p, int s, cudaStream_t st) {
+  FieldSlot& f = p->slot[s];
+  BSK_REQUIRE(f.painted, BSK_ERR_STATE, "field slot " + std::to_string(s) + " was not painted");
+  if (f.fields_ok) return;
+  if (!f.fields) f.fields = (float*)dmalloc((size_t)p->n_alloc() * p->K * sizeof(float));
+  bind_work(p, p->c2r, st);
+  for (int s0 = 0; s0 < p->n; s0 += p->chunk) {
+    int ns = std::min(p->chunk, p->n - s0);
+    launch_filter(p, f.spec, s0, ns, p->chunk_spec, st);
+    if (ns < p->chunk)  // the batched plan transforms `chunk` spectra: clear the unused tail
+      BSK_CHECK_CUDA(cudaMemsetAsync(p->chunk_spec + (size_t)ns * p->Mh, 0,
+                                     (size_t)(p->chunk - ns) * p->Mh * sizeof(cufftComplex),
+                                     st));
+    BSK_CHECK_CUFFT(cufftExecC2R(p->c2r, p->chunk_spec, f.fields + (size_t)s0 * p->K));
+  }
+  f.fields_ok = true;
+  f.split_ok = false;
+}
+
+void ensure_split(bsk_plan* p, int s, cudaStream_t st) {
+  FieldSlot& f = p->slot[s];
+  ensure_fields(p, s, st);
+  if (f.split_ok) return;
+  size_t n = (size_t)p->n_alloc() * p->K;
+  if (!f.hi) f.hi = (__nv_bfloat16*)dmalloc(n * sizeof(__nv_bfloat16));
+  if (!f.lo) f.lo = (__nv_bfloat16*)dmalloc(n * sizeof(__nv_bfloat16));
+  launch_split(f.fields, f.hi, f.lo, (int64_t)n, st);
+  f.split_ok = true;
+}
+
+void free_slot(FieldSlot& f) {
+  if (f.spec) cudaFree(f.spec);
+  if (f.fields) cudaFree(f.fields);
+  if (f.hi) cudaFree(f.hi);
+  if (f.lo) cudaFree(f.lo);
+  f = FieldSlot{};
+}
+
+void destroy_plan(bsk_plan* p) {
+  if (!p) return;
+  DeviceGuard g(p->device);
+  cudaDeviceSynchronize();
+  for (auto& s : p->slot) free_slot(s);
+  if (p->table) cudaFree(p->table);
+  if (p->d_edges) cudaFree(p->d_edges);
+  if (p->chunk_spec) cudaFree(p->chunk_spec);
+  if (p->r2c_ok) cufftDestroy(p->r2c);
+  if (p->c2r_ok) cufftDestroy(p->c2r);
+  if (p->z2d_ok) cufftDestroy(p->z2d);
+  if (p->work) cudaFree(p->work);
+  delete p;
+}
+
+// Scatter results of the first occurrence of a repeated triangle to its copies.
+__global__ void copy_dups_kernel(int n, const int2* pairs, double* v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[pairs[i].x] = v[pairs[i].y];
+}
+
+void copy_dups(const bsk_triset* set, double* v, cudaStream_t st) {
+  if (set->n_dups == 0) return;
+  int n = set->n_dups;
+  copy_dups_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, set->dups, v);
+  BSK_CHECK_CUDA(cudaGetLastError());
+}
+
+void contract_dispatch(bsk_plan* p, const bsk_triset* set, const float* f1, const float* f2,
+                       const float* f3, const __nv_bfloat16* hi, const __nv_bfloat16* lo,
+                       int64_t K, int64_t k0, int64_t k1, int precision, double* out,
+                       cudaStream_t st) {
+  BSK_CHECK_CUDA(cudaMemsetAsync(out, 0, (size_t)set->T * sizeof(double), st));
+  switch (precision) {
+    case BSK_PREC_FP64:
+      launch_contract_simt_f64(set->sched, f1, f2, f3, p->n, K, k0, k1, out, p->num_sms, st);
+      break;
+    case BSK_PREC_FP32:
+      launch_contract_simt_f32(set->sched, f1, f2, f3, p->n, K, k0, k1, out, p->num_sms, st);
+      break;
+    case BSK_PREC_BF16X3:
+    case BSK_PREC_BF16:
+      launch_contract_tc(set->sched, f1, f2, hi, lo, p->n, K, k0, k1,
+                         precision == BSK_PREC_BF16X3 ? 3 : 1, out, p->num_sms, st);
+      break;
+    default:
+      throw Error{BSK_ERR_ARG, "unknown precision " + std::to_string(precision)};
+  }
+  copy_dups(set, out, st);
+}
+
+void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int precision,
+               int64_t k0, int64_t k1, double* out, cudaStream_t st) {
+  BSK_REQUIRE(p && set && out, BSK_ERR_ARG, "NULL argument");
+  BSK_REQUIRE(set->plan == p, BSK_ERR_ARG, "triangle set belongs to another plan");
+  BSK_REQUIRE(a >= 0 && a < 3 && b >= 0 && b < 3 && c >= 0 && c < 3, BSK_ERR_ARG,
+              "slot must be 0, 1 or 2");
+  BSK_REQUIRE(0 <= k0 && k0 <= k1 && k1 <= p->K, BSK_ERR_ARG, "bad point range");
+  if (set->T == 0) return;
+  ensure_fields(p, a, st);
+  ensure_fields(p, b, st);
+  ensure_fields(p, c, st);
+  const __nv_bfloat16 *hi = nullptr, *lo = nullptr;
+  if (precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16) {
+    BSK_REQUIRE(k0 % 64 == 0, BSK_ERR_ARG, "tensor-core ranges must start at a multiple of 64");
+    ensure_split(p, c, st);
+    hi = p->slot[c].hi;
+    lo = p->slot[c].lo;
+  }
+  contract_dispatch(p, set, p->slot[a].fields, p->slot[b].fields, p->slot[c].fields, hi, lo,
+                    p->K, k0, k1, precision, out, st);
+  const double scale = std::pow(p->L, 6) / (double)p->K;
+  launch_scale(out, set->T, scale, st);
+}
+
+}  // namespace
+
+void set_error(const std::string& msg) { g_err = msg; }
+const std::string& get_error() { return g_err; }
+
+}  // namespace bsk
+
+using namespace bsk;
+
+extern "C" {
+
+int bsk_version(void) { return 100; }
+
+int bsk_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return BSK_ERR_ARG;
+  size_t n = std::min(len - 1, g_err.size());
+  std::memcpy(buf, g_err.data(), n);
+  buf[n] = '\0';
+  return BSK_OK;
+}
+
+int bsk_plan_create(int nmesh, double box_size, int n_shells, const double* shell_edges,
+                    int grid_mode, size_t mem_budget, bsk_plan** out) {
+  return guarded([&] {
+    BSK_REQUIRE(out, BSK_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    BSK_REQUIRE(nmesh >= 2 && nmesh % 2 == 0, BSK_ERR_ARG, "Nmesh must be even and >= 2");
+    BSK_REQUIRE(nmesh <= 2048, BSK_ERR_UNSUPPORTED, "Nmesh above 2048");
+    BSK_REQUIRE(std::isfinite(box_size) && box_size > 0, BSK_ERR_ARG, "BoxSize must be > 0");
+    BSK_REQUIRE(n_shells >= 1 && n_shells <= 255, BSK_ERR_ARG, "need 1..255 shells");
+    BSK_REQUIRE(shell_edges, BSK_ERR_ARG, "shell_edges is NULL");
+    BSK_REQUIRE(grid_mode == BSK_GRID_REDUCED || grid_mode == BSK_GRID_NATIVE, BSK_ERR_ARG,
+                "bad grid mode");
+    std::unique_ptr<bsk_plan> p(new bsk_plan());
+    BSK_CHECK_CUDA(cudaGetDevice(&p->device));
+    BSK_CHECK_CUDA(cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount,
+                                          p->device));
+    p->N = nmesh;
+    p->L = box_size;
+    p->n = n_shells;
+    p->mem_budget = mem_budget;
+    p->edges.assign(shell_edges, shell_edges + 2 * n_shells);
+    double hi_max = 0.0;
+    for (int s = 0; s < n_shells; ++s) {
+      BSK_REQUIRE(std::isfinite(p->edges[2 * s]) && std::isfinite(p->edges[2 * s + 1]),
+                  BSK_ERR_ARG, "non-finite shell edge");
+      if (p->edges[2 * s + 1] >= p->edges[2 * s]) hi_max = std::max(hi_max, p->edges[2 * s + 1]);
+    }
+    const double kf = 2.0 * 3.14159265358979323846 / box_size;
+    double qd = std::floor(hi_max / kf * (1.0 + 1e-9));
+    int qmax = (int)std::min<double>(qd, nmesh / 2);
+    p->qmax = qmax;
+    p->Ng = choose_grid(nmesh, qmax, grid_mode);
+    p->K = (int64_t)p->Ng * p->Ng * p->Ng;
+    p->Mh = (int64_t)p->Ng * p->Ng * (p->Ng / 2 + 1);
+    p->chunk = std::min(n_shells, 8);
+
+    p->table = (uint16_t*)dmalloc((size_t)p->Mh * sizeof(uint16_t));
+    p->d_edges = (double*)dmalloc((size_t)2 * n_shells * sizeof(double));
+    BSK_CHECK_CUDA(cudaMemcpy(p->d_edges, p->edges.data(), 2 * n_shells * sizeof(double),
+                              cudaMemcpyHostToDevice));
+    unsigned long long* d_counts = (unsigned long long*)dmalloc(n_shells * sizeof(unsigned long long));
+    int* d_flag = (int*)dmalloc(2 * sizeof(int));
+    BSK_CHECK_CUDA(cudaMemset(d_counts, 0, n_shells * sizeof(unsigned long long)));
+    BSK_CHECK_CUDA(cudaMemset(d_flag, 0, 2 * sizeof(int)));
+    launch_shell_table(p.get(), d_counts, d_flag, 0);
+    std::vector<unsigned long long> hc(n_shells);
+    int hf[2] = {0, 0};
+    BSK_CHECK_CUDA(cudaMemcpy(hc.data(), d_counts, n_shells * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost));
+    BSK_CHECK_CUDA(cudaMemcpy(hf, d_flag, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+    cudaFree(d_counts);
+    cudaFree(d_flag);
+    BSK_REQUIRE(hf[0] == 0, BSK_ERR_UNSUPPORTED,
+                "a Fourier mode lies in shells that are not consecutive; give shells sorted "
+                "by edge with overlaps only between neighbours");
+    BSK_REQUIRE(hf[1] <= qmax || p->Ng == p->N, BSK_ERR_CUDA,
+                "internal: shell mode beyond the reduced-grid bound");
+    p->counts.assign(hc.begin(), hc.end());
+
+    make_r2c(p.get());
+    make_c2r(p.get());
+    p->chunk_spec = (cufftComplex*)dmalloc((size_t)p->chunk * p->Mh * sizeof(cufftComplex));
+    *out = p.release();
+  });
+}
+
+int bsk_plan_destroy(bsk_plan* plan) {
+  return guarded([&] { destroy_plan(plan); });
+}
+
+int bsk_plan_query(const bsk_plan* p, int64_t* info) {
+  return guarded([&] {
+    BSK_REQUIRE(p && info, BSK_ERR_ARG, "NULL argument");
+    int64_t fp = (int64_t)p->Mh * 2 + (int64_t)p->chunk * p->Mh * 8;
+    for (const auto& s : p->slot) {
+      if (s.spec) fp += p->Mh * 8;
+      if (s.fields) fp += (int64_t)p->n_alloc() * p->K * 4;
+      if (s.hi) fp += (int64_t)p->n_alloc() * p->K * 4;
+    }
+    fp += (int64_t)p->work_bytes;
+    info[BSK_INFO_NMESH] = p->N;
+    info[BSK_INFO_NGRID] = p->Ng;
+    info[BSK_INFO_NSHELLS] = p->n;
+    info[BSK_INFO_QMAX] = p->qmax;
+    info[BSK_INFO_FOOTPRINT] = fp;
+    info[BSK_INFO_CHUNK] = p->chunk;
+    info[BSK_INFO_DEVICE] = p->device;
+    info[7] = 0;
+  });
+}
+
+int bsk_shell_mode_counts(const bsk_plan* p, int64_t* counts) {
+  return guarded([&] {
+    BSK_REQUIRE(p && counts, BSK_ERR_ARG, "NULL argument");
+    std::copy(p->counts.begin(), p->counts.end(), counts);
+  });
+}
+
+int bsk_triset_create(bsk_plan* p, int64_t n_tri, const int32_t* tri, bsk_triset** out) {
+  return guarded([&] {
+    BSK_REQUIRE(p && out, BSK_ERR_ARG, "NULL argument");
+    BSK_REQUIRE(n_tri >= 0 && (n_tri == 0 || tri), BSK_ERR_ARG, "bad triangle list");
+    BSK_REQUIRE(n_tri < (1ll << 31), BSK_ERR_UNSUPPORTED, "too many triangles");
+    *out = nullptr;
+    DeviceGuard g(p->device);
+    std::unique_ptr<bsk_triset> s(new bsk_triset());
+    s->plan = p;
+    s->T = n_tri;
+    std::map<std::tuple<int, int, int>, int> first;
+    std::vector<HostTriangle> uniq;
+    std::vector<int2> dups;
+    std::vector<HostTriangle> sched_tri;
+    std::vector<int> sched_t;
+    for (int64_t t = 0; t < n_tri; ++t) {
+      HostTriangle h{tri[3 * t], tri[3 * t + 1], tri[3 * t + 2]};
+      BSK_REQUIRE(h.i >= 0 && h.j >= 0 && h.l >= 0 && h.i < p->n && h.j < p->n && h.l < p->n,
+                  BSK_ERR_ARG, "triangle " + std::to_string(t) + " has a shell index outside [0, " +
+                                   std::to_string(p->n) + ")");
+      s->tri.push_back(h);
+      s->max_shell = std::max(s->max_shell, std::max(h.i, std::max(h.j, h.l)));
+      auto key = std::make_tuple(h.i, h.j, h.l);
+      auto it = first.find(key);
+      if (it == first.end()) {
+        first.emplace(key, (int)t);
+      } else {
+        dups.push_back(make_int2((int)t, it->second));
+      }
+    }
+    // schedule over unique triangles; map entries carry the first index
+    std::vector<HostTriangle> u_tri;
+    std::vector<int> u_idx;
+    {
+      // keep original order of first occurrences
+      std::vector<char> is_first(n_tri, 0);
+      for (auto& kv : first) is_first[kv.second] = 1;
+      for (int64_t t = 0; t < n_tri; ++t)
+        if (is_first[t]) {
+          u_tri.push_back(s->tri[t]);
+          u_idx.push_back((int)t);
+        }
+    }
+    build_schedule(u_tri, p->n, s->sched);
+    // remap map entries (indices into u_tri) to original triangle indices
+    if (!u_tri.empty() && s->sched.n_tiles > 0) {
+      size_t total = 0;
+      for (auto& d : s->sched.h_tiles) total += (size_t)d.nc * kTileRows;
+      std::vector<int32_t> m(total);
+      BSK_CHECK_CUDA(cudaMemcpy(m.data(), s->sched.map, total * sizeof(int32_t),
+                                cudaMemcpyDeviceToHost));
+      for (auto& v : m)
+        if (v >= 0) v = u_idx[v];
+      BSK_CHECK_CUDA(cudaMemcpy(s->sched.map, m.data(), total * sizeof(int32_t),
+                                cudaMemcpyHostToDevice));
+    }
+    if (!dups.empty()) {
+      s->n_dups = (int)dups.size();
+      s->dups = (int2*)dmalloc(dups.size() * sizeof(int2));
+      BSK_CHECK_CUDA(cudaMemcpy(s->dups, dups.data(), dups.size() * sizeof(int2),
+                                cudaMemcpyHostToDevice));
+    }
+    *out = s.release();
+  });
+}
+
+int bsk_triset_destroy(bsk_triset* set) {
+  return guarded([&] {
+    if (!set) return;
+    DeviceGuard g(set->plan->device);
+    set->sched.release();
+    if (set->dups) cudaFree(set->dups);
+    delete set;
+  });
+}
+
+int64_t bsk_triset_size(const bsk_triset* set) { return set ? set->T : -1; }
+
+int bsk_paint(bsk_plan* p, int slot, const float* mesh, void* stream) {
+  return guarded([&] {
+    BSK_REQUIRE(p && mesh, BSK_ERR_ARG, "NULL argument");
+    BSK_REQUIRE(slot >= 0 && slot < 3, BSK_ERR_ARG, "slot must be 0, 1 or 2");
+    DeviceGuard g(p->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    FieldSlot& f = p->slot[slot];
+    size_t fine_elems = (size_t)p->N * p->N * (p->N / 2 + 1);
+    cufftComplex* fine = (cufftComplex*)dmalloc_async(fine_elems * sizeof(cufftComplex), st);
+    bind_work(p, p->r2c, st);
+    BSK_CHECK_CUFFT(cufftExecR2C(p->r2c, const_cast<float*>(mesh), fine));
+    if (!f.spec) f.spec = (cufftComplex*)dmalloc((size_t)p->Mh * sizeof(cufftComplex));
+    launch_extract(p, fine, f.spec, st);
+    BSK_CHECK_CUDA(cudaFreeAsync(fine, st));
+    f.painted = true;
+    f.fields_ok = false;
+    f.split_ok = false;
+  });
+}
+
+int bsk_measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int precision,
+                  double* out, void* stream) {
+  return guarded([&] {
+    BSK_REQUIRE(p, BSK_ERR_ARG, "NULL plan");
+    DeviceGuard g(p->device);
+    measure_b(p, set, a, b, c, precision, 0, p->K, out, (cudaStream_t)stream);
+  });
+}
+
+int bsk_measure_b_range(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int precision,
+                        int64_t k_begin, int64_t k_end, double* out, void* stream) {
+  return guarded([&] {
+    BSK_REQUIRE(p, BSK_ERR_ARG, "NULL plan");
+    DeviceGuard g(p->device);
+    measure_b(p, set, a, b, c, precision, k_begin, k_end, out, (cudaStream_t)stream);
+  });
+}
+
+int bsk_contract(bsk_plan* p, const bsk_triset* set, const float* f1, const float* f2,
+                 const float* f3, int64_t K, int precision, double* out, void* stream) {
+  return guarded([&] {
+    BSK_REQUIRE(p && set && f1 && f2 && f3 && out, BSK_ERR_ARG, "NULL argument");
+    BSK_REQUIRE(set->plan == p, BSK_ERR_ARG, "triangle set belongs to another plan");
+    BSK_REQUIRE(K > 0 && K % 8 == 0, BSK_ERR_ARG, "k_points must be a positive multiple of 8");
+    DeviceGuard g(p->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (set->T == 0) return;
+    __nv_bfloat16 *hi = nullptr, *lo = nullptr;
+    if (precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16) {
+      size_t n = (size_t)p->n * K;
+      hi = (__nv_bfloat16*)dmalloc_async(n * sizeof(__nv_bfloat16), st);
+      lo = (__nv_bfloat16*)dmalloc_async(n * sizeof(__nv_bfloat16), st);
+      launch_split(f3, hi, lo, (int64_t)n, st);
+    }
+    contract_dispatch(p, set, f1, f2, f3, hi, lo, K, 0, K, precision, out, st);
+    if (hi) BSK_CHECK_CUDA(cudaFreeAsync(hi, st));
+    if (lo) BSK_CHECK_CUDA(cudaFreeAsync(lo, st));
+  });
+}
+
+int bsk_gridinfo(bsk_plan* p, const bsk_triset* set, double* ntri, double* kmean,
+                 void* stream) {
+  return guarded([&] {
+    BSK_REQUIRE(p && set && ntri && kmean, BSK_ERR_ARG, "NULL argument");
+    BSK_REQUIRE(set->plan == p, BSK_ERR_ARG, "triangle set belongs to another plan");
+    DeviceGuard g(p->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (set->T == 0) return;
+    make_z2d(p);
+    bind_work(p, p->z2d, st);
+    const size_t fbytes = (size_t)p->n_alloc() * p->K * sizeof(double);
+    double* nf = (double*)dmalloc_async(fbytes, st);
+    double* kf = (double*)dmalloc_async(fbytes, st);
+    cufftDoubleComplex* spec = (cufftDoubleComplex*)dmalloc_async(
+        (size_t)p->chunk * p->Mh * sizeof(cufftDoubleComplex), st);
+    for (int kw = 0; kw < 2; ++kw) {
+      double* dst = kw ? kf : nf;
+      for (int s0 = 0; s0 < p->n; s0 += p->chunk) {
+        int ns = std::min(p->chunk, p->n - s0);
+        if (ns < p->chunk)
+          BSK_CHECK_CUDA(cudaMemsetAsync(
+              spec + (size_t)ns * p->Mh, 0,
+              (size_t)(p->chunk - ns) * p->Mh * sizeof(cufftDoubleComplex), st));
+        launch_filter_indicator(p, s0, ns, kw, spec, st);
+        BSK_CHECK_CUFFT(cufftExecZ2D(p->z2d, spec, dst + (size_t)s0 * p->K));
+      }
+    }
+    BSK_CHECK_CUDA(cudaFreeAsync(spec, st));
+    double* s1 = (double*)dmalloc_async((size_t)3 * set->T * sizeof(double), st);
+    double* s2 = s1 + set->T;
+    double* s3 = s2 + set->T;
+    auto run = [&](const double* a, const double* b, const double* c, double* o) {
+      BSK_CHECK_CUDA(cudaMemsetAsync(o, 0, (size_t)set->T * sizeof(double), st));
+      launch_contract_simt_d64(set->sched, a, b, c, p->n, p->K, 0, p->K, o, p->num_sms, st);
+      copy_dups(set, o, st);
+    };
+    run(nf, nf, nf, ntri);
+    run(kf, nf, nf, s1);
+    run(nf, kf, nf, s2);
+    run(nf, nf, kf, s3);
+    launch_gridinfo_finish(set->T, 1.0 / (double)p->K, ntri, s1, s2, s3, kmean, st);
+    BSK_CHECK_CUDA(cudaFreeAsync(s1, st));
+    BSK_CHECK_CUDA(cudaFreeAsync(nf, st));
+    BSK_CHECK_CUDA(cudaFreeAsync(kf, st));
+  });
+}
+
+int bsk_normalize(int64_t n, const double* b, const double* ntri, double* out, void* stream) {
+  return guarded([&] {
+    BSK_REQUIRE(n >= 0 && (n == 0 || (b && ntri && out)), BSK_ERR_ARG, "bad argument");
+    if (n) launch_normalize(n, b, ntri, out, (cudaStream_t)stream);
+  });
+}
+
+int bsk_copy_field(bsk_plan* p, int slot, int shell, float* dst, void* stream) {
+  return guarded([&] {
+    BSK_REQUIRE(p && dst, BSK_ERR_ARG, "NULL argument");
+    BSK_REQUIRE(slot >= 0 && slot < 3 && shell >= 0 && shell < p->n, BSK_ERR_ARG,
+                "bad slot or shell");
+    DeviceGuard g(p->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    ensure_fields(p, slot, st);
+    BSK_CHECK_CUDA(cudaMemcpyAsync(dst, p->slot[slot].fields + (size_t)shell * p->K,
+                                   (size_t)p->K * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  });
+}
+
+int bsk_sync_check(void* stream) {
+  return guarded([&] {
+    BSK_CHECK_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    if (tc_error_flag(true))
+      throw Error{BSK_ERR_TIMEOUT, "tcgen05 contraction: a bounded pipeline wait expired"};
+  });
+}
+
+}  // extern "C"

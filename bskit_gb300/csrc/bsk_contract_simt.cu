@@ -1,0 +1,174 @@
+// SIMT triple-product contraction: the plain-FP32 path and the FP64 GPU oracle.
+//
+// Work item = (sub-tile of 128 pair rows x 32 third-shell columns, K slice).
+// Per 32-point chunk the block forms the 128 pair products P[r][x] =
+// F1[i_r](x) * F2[j_r](x) and the 32 column values F3[l](x) in shared memory
+// (double buffered, register prefetch of the next chunk), then a 4x4
+// register-tiled outer-product loop accumulates C[r][c] += P[r][x] * F3[c][x].
+// At the end of the slice the tile sums are added to the FP64 output with
+// atomics (only entries that are triangle bins).  Items are ordered slice-major
+// so that blocks running at the same time share field data in L2.
+#include "bsk_internal.cuh"
+
+namespace bsk {
+namespace {
+
+constexpr int KC = 32;     // points per chunk
+constexpr int ROWS = 128;  // pair rows per sub-tile
+constexpr int COLS = 32;   // columns per sub-tile
+constexpr int APAD = 4;
+constexpr int BPAD = 4;
+constexpr int THREADS = 256;
+
+template <typename Tin, typename Tacc>
+__device__ __forceinline__ Tacc prod(Tin a, Tin b) {
+  return (Tacc)a * (Tacc)b;
+}
+
+template <typename Tin, typename Tacc>
+__global__ void __launch_bounds__(THREADS) contract_simt_kernel(
+    const TileDesc* __restrict__ tiles, const int2* __restrict__ subs, int n_sub,
+    const int16_t* __restrict__ row_i, const int16_t* __restrict__ row_j,
+    const int32_t* __restrict__ map, const Tin* __restrict__ f1, const Tin* __restrict__ f2,
+    const Tin* __restrict__ f3, int n_shells, int64_t K, int64_t k_begin, int64_t k_end,
+    int64_t slice, int64_t n_slices, double* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char simt_smem[];
+  typedef Tacc ATile[KC][ROWS + APAD];
+  typedef Tacc BTile[KC][COLS + BPAD];
+  ATile* As = reinterpret_cast<ATile*>(simt_smem);
+  BTile* Bs = reinterpret_cast<BTile*>(simt_smem + 2 * sizeof(ATile));
+  const int tid = threadIdx.x;
+  const int tx = tid & 7, ty = tid >> 3;          // micro-tile rows ty*4.., cols tx*4..
+  const int ar = tid & (ROWS - 1), ah = tid >> 7;  // A-gen: row ar, points ah*16 .. +16
+  const int bc = tid >> 3, bp = (tid & 7) * 4;     // B-gen: column bc, points bp .. +4
+  const int64_t n_items = (int64_t)n_sub * n_slices;
+
+  for (int64_t item = blockIdx.x; item < n_items; item += gridDim.x) {
+    const int64_t sl = item / n_sub;
+    const int2 sub = subs[item % n_sub];
+    const TileDesc td = tiles[sub.x];
+    const int c0 = sub.y;
+    const int ri = row_i[td.row_off + ar];
+    const int rj = row_j[td.row_off + ar];
+    const int lcol = td.l0 + c0 + bc;
+    const bool bvalid = (c0 + bc < td.nc) && (lcol < n_shells);
+    const Tin* pa = f1 + (int64_t)(ri >= 0 ? ri : 0) * K;
+    const Tin* pb = f2 + (int64_t)(ri >= 0 ? rj : 0) * K;
+    const Tin* pc = f3 + (int64_t)(bvalid ? lcol : 0) * K;
+    const int64_t x_begin = k_begin + sl * slice;
+    const int64_t x_end = min(k_end, x_begin + slice);
+
+    Tacc acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = (Tacc)0;
+
+    Tacc ra[16], rc[4];
+    auto load = [&](int64_t x0) {
+      const int64_t xa = x0 + ah * 16;
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        int64_t x = xa + e;
+        ra[e] = (ri >= 0 && x < x_end) ? prod<Tin, Tacc>(__ldg(pa + x), __ldg(pb + x)) : (Tacc)0;
+      }
+      const int64_t xc = x0 + bp;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        int64_t x = xc + e;
+        rc[e] = (bvalid && x < x_end) ? (Tacc)__ldg(pc + x) : (Tacc)0;
+      }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+      for (int e = 0; e < 16; ++e) As[buf][ah * 16 + e][ar] = ra[e];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) Bs[buf][bp + e][bc] = rc[e];
+    };
+
+    load(x_begin);
+    store(0);
+    __syncthreads();
+    int buf = 0;
+    for (int64_t x0 = x_begin; x0 < x_end; x0 += KC) {
+      const bool more = x0 + KC < x_end;
+      if (more) load(x0 + KC);
+#pragma unroll 8
+      for (int k = 0; k < KC; ++k) {
+        Tacc a[4], b[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          a[q] = As[buf][k][ty * 4 + q];
+          b[q] = Bs[buf][k][tx * 4 + q];
+        }
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[p][q] += a[p] * b[q];
+      }
+      if (more) store(buf ^ 1);
+      __syncthreads();
+      buf ^= 1;
+    }
+
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      const int r = ty * 4 + p;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int c = c0 + tx * 4 + q;
+        if (c < td.nc) {
+          const int t = map[td.map_off + c * ROWS + r];
+          if (t >= 0) atomicAdd(out + t, (double)acc[p][q]);
+        }
+      }
+    }
+  }
+}
+
+template <typename Tin, typename Tacc>
+void launch_simt(const DeviceSchedule& s, const Tin* f1, const Tin* f2, const Tin* f3,
+                 int n_shells, int64_t K, int64_t k_begin, int64_t k_end, int64_t slice,
+                 double* out, int num_sms, cudaStream_t st) {
+  if (s.n_sub == 0 || k_end <= k_begin) return;
+  const size_t smem = 2 * sizeof(Tacc) * KC * ((ROWS + APAD) + (COLS + BPAD));
+  BSK_CHECK_CUDA(cudaFuncSetAttribute(contract_simt_kernel<Tin, Tacc>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  BSK_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, contract_simt_kernel<Tin, Tacc>, THREADS, smem));
+  if (per_sm < 1) per_sm = 1;
+  const int64_t n_slices = (k_end - k_begin + slice - 1) / slice;
+  const int64_t n_items = n_slices * s.n_sub;
+  int64_t grid = (int64_t)num_sms * per_sm;
+  if (grid > n_items) grid = n_items;
+  contract_simt_kernel<Tin, Tacc><<<(unsigned)grid, THREADS, smem, st>>>(
+      s.tiles, s.subs, s.n_sub, s.row_i, s.row_j, s.map, f1, f2, f3, n_shells, K, k_begin, k_end,
+      slice, n_slices, out);
+  BSK_CHECK_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+// FP32 products and tile sums, 4096-point slices, FP64 cross-slice sum.
+void launch_contract_simt_f32(const DeviceSchedule& s, const float* f1, const float* f2,
+                              const float* f3, int n_shells, int64_t K, int64_t k_begin,
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st) {
+  launch_simt<float, float>(s, f1, f2, f3, n_shells, K, k_begin, k_end, 4096, out, num_sms, st);
+}
+
+// FP64 products and sums of FP32 fields (the GPU oracle of the precision study).
+void launch_contract_simt_f64(const DeviceSchedule& s, const float* f1, const float* f2,
+                              const float* f3, int n_shells, int64_t K, int64_t k_begin,
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st) {
+  launch_simt<float, double>(s, f1, f2, f3, n_shells, K, k_begin, k_end, 65536, out, num_sms, st);
+}
+
+// FP64 fields (grid information).
+void launch_contract_simt_d64(const DeviceSchedule& s, const double* f1, const double* f2,
+                              const double* f3, int n_shells, int64_t K, int64_t k_begin,
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st) {
+  launch_simt<double, double>(s, f1, f2, f3, n_shells, K, k_begin, k_end, 65536, out, num_sms, st);
+}
+
+}  // namespace bsk

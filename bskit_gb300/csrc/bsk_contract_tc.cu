@@ -1,0 +1,544 @@
+// tcgen05 (5th-gen tensor core) triple-product contraction, bf16x3 / bf16.
+//
+//   C[(i,j), l] += sum_x P_ij(x) * F3_l(x),   P_ij = F1_i * F2_j  (FP32, formed on chip)
+//
+// One persistent CTA per SM walks work items (tile of 128 pair rows x nc <= 64
+// columns, K slice of SLICE points), slice-major so that the CTAs running at
+// the same time share field data in L2.  Per 64-point chunk:
+//   * warp 0 (one lane) TMA-loads into a 4-stage SMEM ring the bf16 hi / lo
+//     tiles of the column fields (SWIZZLE_128B, K-major: the UMMA B operand)
+//     and the FP32 tile(s) of the pair-factor shells (one 64-shell tile when a
+//     single range covers both factors of every row, as for auto spectra);
+//   * warps 6..13 (2 per TMEM lane quadrant, one 32-point half each) read the
+//     row's F1_i, F2_j from SMEM, form P = F1_i*F2_j, split P = hi + lo (bf16,
+//     lo = bf16(fma(a, b, -hi))) and store them with tcgen05.st into a 4-stage
+//     TMEM A-operand ring (lane = GEMM row);
+//   * warp 1 (one lane) issues tcgen05.mma kind::f16 (A from TMEM, B from SMEM)
+//     hi*Bhi + hi*Blo + lo*Bhi (bf16x3) or hi*Bhi (bf16): M=128, N=nc, K=16 x 4.
+//     The tensor core's FP32 accumulate truncates, so an accumulator is only
+//     ever fed ACC_CHUNKS chunks (<= 24 MMAs) and then handed over;
+//   * warps 2..5 drain each finished accumulator with tcgen05.ld, add it into
+//     per-thread FP32 registers (round-to-nearest), and at the end of the slice
+//     add the entries that are triangle bins into the FP64 output (atomics).
+// Every mbarrier wait is bounded (globaltimer); on expiry the kernel records
+// an error flag, stops issuing work, drains its own MMAs and frees TMEM.
+#include <cuda.h>
+
+#include "bsk_internal.cuh"
+
+namespace bsk {
+namespace tc {
+
+constexpr int KCH = 64;                       // points per chunk
+constexpr int ACC_CHUNKS = 2;                 // chunks summed inside one TMEM accumulator
+constexpr int STAGES = 4;                     // SMEM ring
+constexpr int A_STAGES = 4;                   // TMEM A-operand ring
+constexpr int NACC = 2;                       // TMEM accumulators
+constexpr int B_TILE = kMaxCols * 128;        // 8 KB: <= 64 rows x 64 bf16
+constexpr int A_HALF = kMaxSrcRows * 128;     // 8 KB: 64 rows x 32 fp32
+constexpr int A_TILE = 2 * A_HALF;            // 16 KB
+constexpr int STAGE_BYTES = 2 * B_TILE + 2 * A_TILE;  // 48 KB
+constexpr int NUM_WARPS = 14;
+constexpr int THREADS = NUM_WARPS * 32;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t ACC_COL = 0;               // accumulator b at 64 b
+constexpr uint32_t A_COL = 128;               // A stage a at 128 + 64 a: hi +0..31, lo +32..63
+constexpr int64_t SLICE = 16384;              // points per work item
+constexpr unsigned long long kTimeoutNs = 2000000000ull;
+
+struct Bars {
+  uint64_t full[STAGES];
+  uint64_t empty[STAGES];
+  uint64_t afull[A_STAGES];
+  uint64_t aempty[A_STAGES];
+  uint64_t accfull[NACC];
+  uint64_t accempty[NACC];
+  uint64_t done;
+  uint32_t tmem_base;
+};
+
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*bars*/ + 1024 /*align slack*/;
+
+// Tensor maps of one launch: bf16 column fields with 16/32/64-row boxes, FP32 sources.
+struct Maps {
+  CUtensorMap hi16, hi32, hi64, lo16, lo32, lo64, f1, f2;
+};
+
+__device__ int g_tc_error;  // 0 ok, 1 a bounded wait expired
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false when the wait expired or another role already gave up.
+__device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer();
+  while (true) {
+#pragma unroll 1
+    for (int i = 0; i < 32; ++i)
+      if (mbar_try(bar, parity)) return true;
+    if (*(volatile int*)&g_tc_error) return false;
+    if (globaltimer() - t0 > kTimeoutNs) {
+      atomicExch(&g_tc_error, 1);
+      return false;
+    }
+  }
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+// D[tmem] (+)= A[tmem] * B[smem]^T, kind::f16 (bf16 in, f32 accumulate)
+__device__ __forceinline__ void mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc,
+                                       uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(
+          taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+        "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// UMMA shared-memory descriptor: K-major, SWIZZLE_128B, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                    // leading byte offset (16 B, unused for SW128)
+  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset
+  d |= (uint64_t)1 << 46;                    // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                    // layout: SWIZZLE_128B
+  return d;
+}
+// Instruction descriptor: D=F32, A=B=BF16, both K-major, M=128, N=n.
+__host__ __device__ __forceinline__ uint32_t idesc_bf16(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+
+__device__ __forceinline__ void load_cols(uint32_t dst, const CUtensorMap* m16,
+                                          const CUtensorMap* m32, const CUtensorMap* m64,
+                                          uint64_t* bar, int x, int y, int nc) {
+  if (nc == 64) {
+    tma_load_2d(dst, m64, bar, x, y);
+  } else if (nc >= 32) {
+    tma_load_2d(dst, m32, bar, x, y);
+    if (nc == 48) tma_load_2d(dst + 32 * 128, m16, bar, x, y + 32);
+  } else {
+    tma_load_2d(dst, m16, bar, x, y);
+  }
+}
+
+__global__ void __maxnreg__(144)
+    contract_tc_kernel(const __grid_constant__ Maps maps, const TileDesc* __restrict__ tiles,
+                       const int16_t* __restrict__ row_i, const int16_t* __restrict__ row_j,
+                       const int32_t* __restrict__ map, int n_tiles, int same_src,
+                       int64_t k_begin, int64_t k_end, int64_t n_items, int terms,
+                       double* __restrict__ out) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
+  uint8_t* smem = smem_raw + pad;
+  Bars* bars = reinterpret_cast<Bars*>(smem + STAGES * STAGE_BYTES);
+  const uint32_t sbase = raw + pad;
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&bars->full[s], 1);
+      mbar_init(&bars->empty[s], 1 + 8);
+    }
+    for (int a = 0; a < A_STAGES; ++a) {
+      mbar_init(&bars->afull[a], 8);
+      mbar_init(&bars->aempty[a], 1);
+    }
+    for (int b = 0; b < NACC; ++b) {
+      mbar_init(&bars->accfull[b], 1);
+      mbar_init(&bars->accempty[b], 4);
+    }
+    mbar_init(&bars->done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&bars->tmem_base)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = bars->tmem_base;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ TMA producer
+    if (lane == 0) {
+      uint32_t chunk = 0;
+      bool ok = true;
+      for (int64_t item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
+        const int64_t sl = item / n_tiles;
+        const TileDesc td = tiles[item % n_tiles];
+        const bool one_src = same_src && td.i0 == td.j0;
+        const int64_t x_begin = k_begin + sl * SLICE;
+        const int64_t x_end = min(k_end, x_begin + SLICE);
+        const uint32_t bbytes = (uint32_t)((td.nc == 64 ? 64 : td.nc) * 128);
+        const uint32_t bytes = 2 * bbytes + (one_src ? 1u : 2u) * (uint32_t)A_TILE;
+        for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
+          const int s = chunk % STAGES;
+          const uint32_t ph = (chunk / STAGES) & 1;
+          if (!mbar_wait(&bars->empty[s], ph ^ 1)) { ok = false; break; }
+          mbar_arrive_tx(&bars->full[s], bytes);
+          const uint32_t st = sbase + s * STAGE_BYTES;
+          const int xi = (int)x;
+          load_cols(st, &maps.hi16, &maps.hi32, &maps.hi64, &bars->full[s], xi, td.l0, td.nc);
+          load_cols(st + B_TILE, &maps.lo16, &maps.lo32, &maps.lo64, &bars->full[s], xi, td.l0,
+                    td.nc);
+          for (int h = 0; h < 2; ++h) {
+            tma_load_2d(st + 2 * B_TILE + h * A_HALF, &maps.f1, &bars->full[s], xi + 32 * h,
+                        td.i0);
+            if (!one_src)
+              tma_load_2d(st + 2 * B_TILE + A_TILE + h * A_HALF, &maps.f2, &bars->full[s],
+                          xi + 32 * h, td.j0);
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      uint32_t chunk = 0, grp = 0;
+      bool ok = true;
+      for (int64_t item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
+        const int64_t sl = item / n_tiles;
+        const TileDesc td = tiles[item % n_tiles];
+        const int64_t x_begin = k_begin + sl * SLICE;
+        const int64_t x_end = min(k_end, x_begin + SLICE);
+        const uint32_t idesc = idesc_bf16(td.nc);
+        int in_grp = 0;
+        uint32_t d_tmem = 0, b = 0, accum = 0;
+        for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
+          if (in_grp == 0) {
+            b = grp % NACC;
+            if (!mbar_wait(&bars->accempty[b], ((grp / NACC) & 1) ^ 1)) { ok = false; break; }
+            tc_fence_after();
+            d_tmem = tmem + ACC_COL + b * 64;
+            accum = 0;
+          }
+          const int s = chunk % STAGES;
+          const uint32_t ph = (chunk / STAGES) & 1;
+          const uint32_t a = chunk % A_STAGES;
+          const uint32_t aph = (chunk / A_STAGES) & 1;
+          if (!mbar_wait(&bars->full[s], ph)) { ok = false; break; }
+          if (!mbar_wait(&bars->afull[a], aph)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t st = sbase + s * STAGE_BYTES;
+          const uint32_t a_hi = tmem + A_COL + a * 64;
+          const uint32_t a_lo = a_hi + 32;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const uint64_t bhi = desc_sw128(st + 32 * k);
+            const uint64_t blo = desc_sw128(st + B_TILE + 32 * k);
+            mma_ts(d_tmem, a_hi + 8 * k, bhi, idesc, accum);
+            accum = 1;
+            if (terms >= 3) {
+              mma_ts(d_tmem, a_hi + 8 * k, blo, idesc, 1);
+              mma_ts(d_tmem, a_lo + 8 * k, bhi, idesc, 1);
+            }
+          }
+          tc_commit(&bars->empty[s]);
+          tc_commit(&bars->aempty[a]);
+          if (++in_grp == ACC_CHUNKS || x + KCH >= x_end) {
+            tc_commit(&bars->accfull[b]);
+            ++grp;
+            in_grp = 0;
+          }
+        }
+      }
+      // all MMAs of this CTA complete before TMEM is released
+      tc_commit(&bars->done);
+      mbar_wait(&bars->done, 0);
+    }
+  } else if (warp < 6) {
+    // ------------------------------------------------------------ accumulator drain
+    const int qd = warp & 3;
+    const int r = qd * 32 + lane;
+    const uint32_t taddr = tmem + ((uint32_t)(qd * 32) << 16);
+    uint32_t grp = 0;
+    bool ok = true;
+    for (int64_t item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
+      const int64_t sl = item / n_tiles;
+      const TileDesc td = tiles[item % n_tiles];
+      const int64_t x_begin = k_begin + sl * SLICE;
+      const int64_t x_end = min(k_end, x_begin + SLICE);
+      const int64_t nch = (x_end - x_begin + KCH - 1) / KCH;
+      const int64_t ngrp = (nch + ACC_CHUNKS - 1) / ACC_CHUNKS;
+      float acc[kMaxCols];
+#pragma unroll
+      for (int c = 0; c < kMaxCols; ++c) acc[c] = 0.f;
+      for (int64_t g = 0; g < ngrp; ++g, ++grp) {
+        const uint32_t b = grp % NACC;
+        if (!__all_sync(0xffffffffu, mbar_wait(&bars->accfull[b], (grp / NACC) & 1))) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+#pragma unroll
+        for (int cc = 0; cc < kMaxCols / 16; ++cc) {
+          if (cc * 16 < td.nc) {
+            uint32_t v[16];
+            tmem_ld16(taddr + ACC_COL + b * 64 + cc * 16, v);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) acc[cc * 16 + e] += __uint_as_float(v[e]);
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&bars->accempty[b]);
+      }
+      if (!ok) break;
+      const int32_t* mp = map + td.map_off + r;
+#pragma unroll
+      for (int c = 0; c < kMaxCols; ++c) {
+        if (c < td.nc) {
+          const int t = __ldg(mp + c * kTileRows);
+          if (t >= 0) atomicAdd(out + t, (double)acc[c]);
+        }
+      }
+    }
+  } else {
+    // ------------------------------------------------------------ A-operand producers
+    const int qd = warp & 3;
+    const int half = (warp - 6) >> 2;
+    const int r = qd * 32 + lane;
+    const uint32_t tlane = (uint32_t)(qd * 32) << 16;
+    uint32_t chunk = 0;
+    bool ok = true;
+    for (int64_t item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
+      const int64_t sl = item / n_tiles;
+      const TileDesc td = tiles[item % n_tiles];
+      const bool one_src = same_src && td.i0 == td.j0;
+      const int64_t x_begin = k_begin + sl * SLICE;
+      const int64_t x_end = min(k_end, x_begin + SLICE);
+      const int ri = row_i[td.row_off + r];
+      const int rj = row_j[td.row_off + r];
+      const bool valid = ri >= 0;
+      const int pi = valid ? ri - td.i0 : 0;
+      const int pj = valid ? rj - td.j0 : 0;
+      const int src2 = one_src ? 0 : A_TILE;
+      for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
+        const int s = chunk % STAGES;
+        const uint32_t ph = (chunk / STAGES) & 1;
+        const uint32_t a = chunk % A_STAGES;
+        const uint32_t aph = (chunk / A_STAGES) & 1;
+        if (!__all_sync(0xffffffffu, mbar_wait(&bars->full[s], ph))) { ok = false; break; }
+        if (!__all_sync(0xffffffffu, mbar_wait(&bars->aempty[a], aph ^ 1))) { ok = false; break; }
+        tc_fence_after();
+        const uint8_t* st = smem + s * STAGE_BYTES;
+        const uint8_t* row1 = st + 2 * B_TILE + half * A_HALF + pi * 128;
+        const uint8_t* row2 = st + 2 * B_TILE + src2 + half * A_HALF + pj * 128;
+        const uint32_t a_hi = tmem + tlane + A_COL + a * 64 + half * 16;
+#pragma unroll
+        for (int sub = 0; sub < 2; ++sub) {
+          uint32_t hi[8], lo[8];
+          if (valid) {
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) {
+              const int c = sub * 4 + c4;  // logical 16-B chunk (4 floats)
+              const float4 va =
+                  *reinterpret_cast<const float4*>(row1 + ((c ^ (pi & 7)) << 4));
+              const float4 vb =
+                  *reinterpret_cast<const float4*>(row2 + ((c ^ (pj & 7)) << 4));
+              const float p0 = va.x * vb.x, p1 = va.y * vb.y;
+              const float p2 = va.z * vb.z, p3 = va.w * vb.w;
+              const uint32_t h01 = pack_bf16(p0, p1), h23 = pack_bf16(p2, p3);
+              const float g0 = __uint_as_float(h01 << 16), g1 = __uint_as_float(h01 & 0xFFFF0000u);
+              const float g2 = __uint_as_float(h23 << 16), g3 = __uint_as_float(h23 & 0xFFFF0000u);
+              hi[2 * c4] = h01;
+              hi[2 * c4 + 1] = h23;
+              lo[2 * c4] = pack_bf16(fmaf(va.x, vb.x, -g0), fmaf(va.y, vb.y, -g1));
+              lo[2 * c4 + 1] = pack_bf16(fmaf(va.z, vb.z, -g2), fmaf(va.w, vb.w, -g3));
+            }
+          } else {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) hi[e] = lo[e] = 0u;
+          }
+          tmem_st8(a_hi + sub * 8, hi);
+          tmem_st8(a_hi + 32 + sub * 8, lo);
+        }
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(&bars->afull[a]);
+          mbar_arrive(&bars->empty[s]);
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    BSK_CHECK_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                                    cudaEnableDefault, &q));
+    BSK_REQUIRE(q == cudaDriverEntryPointSuccess && p, BSK_ERR_CUDA,
+                "cuTensorMapEncodeTiled entry point unavailable");
+    fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// 2D map over a [rows][K] array: box = {box_x elements, box_y rows}, SWIZZLE_128B.
+void make_map(CUtensorMap* m, CUtensorMapDataType dt, int esize, const void* base, int64_t K,
+              int rows, int box_x, int box_y) {
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)K * esize};
+  cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(m, dt, 2, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  BSK_REQUIRE(r == CUDA_SUCCESS, BSK_ERR_CUDA,
+              "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
+}  // namespace tc
+
+void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f2,
+                        const __nv_bfloat16* f3_hi, const __nv_bfloat16* f3_lo, int n_shells,
+                        int64_t K, int64_t k_begin, int64_t k_end, int terms, double* out,
+                        int num_sms, cudaStream_t st) {
+  if (s.n_tiles == 0 || k_end <= k_begin) return;
+  BSK_REQUIRE(k_begin % tc::KCH == 0, BSK_ERR_ARG, "k_begin must be a multiple of 64");
+  BSK_REQUIRE(K < (int64_t)1 << 31, BSK_ERR_UNSUPPORTED, "grid too large for 32-bit TMA x");
+  BSK_REQUIRE(K % 8 == 0, BSK_ERR_UNSUPPORTED, "K must be a multiple of 8");
+  tc::Maps m;
+  const auto BF = CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  tc::make_map(&m.hi16, BF, 2, f3_hi, K, n_shells, 64, 16);
+  tc::make_map(&m.hi32, BF, 2, f3_hi, K, n_shells, 64, 32);
+  tc::make_map(&m.hi64, BF, 2, f3_hi, K, n_shells, 64, 64);
+  tc::make_map(&m.lo16, BF, 2, f3_lo, K, n_shells, 64, 16);
+  tc::make_map(&m.lo32, BF, 2, f3_lo, K, n_shells, 64, 32);
+  tc::make_map(&m.lo64, BF, 2, f3_lo, K, n_shells, 64, 64);
+  tc::make_map(&m.f1, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, f1, K, n_shells, 32, 64);
+  tc::make_map(&m.f2, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, f2, K, n_shells, 32, 64);
+  static bool attr_set = false;
+  if (!attr_set) {
+    BSK_CHECK_CUDA(cudaFuncSetAttribute(tc::contract_tc_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        tc::SMEM_BYTES));
+    attr_set = true;
+  }
+  const int64_t n_slices = (k_end - k_begin + tc::SLICE - 1) / tc::SLICE;
+  const int64_t n_items = n_slices * s.n_tiles;
+  int64_t grid = num_sms;
+  if (grid > n_items) grid = n_items;
+  tc::contract_tc_kernel<<<(unsigned)grid, tc::THREADS, tc::SMEM_BYTES, st>>>(
+      m, s.tiles, s.row_i, s.row_j, s.map, s.n_tiles, f1 == f2 ? 1 : 0, k_begin, k_end,
+      n_items, terms, out);
+  BSK_CHECK_CUDA(cudaGetLastError());
+}
+
+int tc_error_flag(bool reset) {
+  int v = 0;
+  BSK_CHECK_CUDA(cudaMemcpyFromSymbol(&v, tc::g_tc_error, sizeof(int)));
+  if (reset && v) {
+    int z = 0;
+    BSK_CHECK_CUDA(cudaMemcpyToSymbol(tc::g_tc_error, &z, sizeof(int)));
+  }
+  return v;
+}
+
+}  // namespace bsk

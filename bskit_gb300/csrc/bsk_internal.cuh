@@ -1,0 +1,182 @@
+// Internal declarations of the GB300 bispectrum engine (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/bskit_gb300.h"
+
+namespace bsk {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string& msg);
+const std::string& get_error();
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define BSK_CHECK_CUDA(expr)                                                             \
+  do {                                                                                   \
+    cudaError_t _e = (expr);                                                             \
+    if (_e != cudaSuccess)                                                               \
+      throw ::bsk::Error{BSK_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)}; \
+  } while (0)
+
+#define BSK_CHECK_CUFFT(expr)                                                       \
+  do {                                                                              \
+    cufftResult _r = (expr);                                                        \
+    if (_r != CUFFT_SUCCESS)                                                        \
+      throw ::bsk::Error{BSK_ERR_CUFFT, std::string(#expr) + ": cufft status " +    \
+                                            std::to_string((int)_r)};               \
+  } while (0)
+
+#define BSK_REQUIRE(cond, code, msg)                          \
+  do {                                                        \
+    if (!(cond)) throw ::bsk::Error{(code), std::string(msg)}; \
+  } while (0)
+
+// ---------------------------------------------------------------- schedule
+// Rows of a tile are (i, j) shell pairs; columns are a contiguous range of
+// third shells [l0, l0 + nc).  One tile = 128 rows (the tcgen05 M).
+constexpr int kTileRows = 128;
+constexpr int kMaxCols = 64;    // accumulator columns per tile (register budget of the drain)
+constexpr int kMaxSrcRows = 64; // shells per A-source range (one 64-row TMA box)
+
+struct TileDesc {
+  int i0, j0, l0;     // first shell of the F1 rows range, F2 rows range, F3 column range
+  int ni, nj, nc;     // extents (nc multiple of 16 <= 64; ni, nj <= 64; i0 == j0 when one
+                      // 64-shell range covers both pair factors)
+  int nrows;          // valid rows
+  int row_off;        // offset of this tile's 128 row entries
+  int map_off;        // offset of this tile's nc*128 map entries, layout [c][r]
+  int pad;
+};
+
+struct DeviceSchedule {
+  int n_tiles = 0;
+  int sum_nc = 0;
+  TileDesc* tiles = nullptr;   // device
+  int16_t* row_i = nullptr;    // device, absolute shell index, -1 = padding row
+  int16_t* row_j = nullptr;
+  int32_t* map = nullptr;      // device, triangle index or -1
+  int2* subs = nullptr;        // device, SIMT sub-tiles (tile, first column), 32 columns each
+  int n_sub = 0;
+  std::vector<TileDesc> h_tiles;
+  void release();
+};
+
+struct HostTriangle {
+  int i, j, l;
+};
+
+// Build the tile schedule for a triangle list (host).  `n_shells` bounds the
+// indices.  Rows with identical (i, j) share one pair product.
+void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSchedule& out);
+
+// ---------------------------------------------------------------- plan
+struct FieldSlot {
+  bool painted = false;
+  cufftComplex* spec = nullptr;   // coarse half spectrum, scaled 1/N^3 (Ng*Ng*(Ng/2+1))
+  float* fields = nullptr;        // [n][K] FP32 shell fields (nullptr until built)
+  __nv_bfloat16* hi = nullptr;    // [n][K] bf16 split (nullptr until built)
+  __nv_bfloat16* lo = nullptr;
+  bool fields_ok = false;
+  bool split_ok = false;
+};
+
+}  // namespace bsk
+
+struct bsk_plan {
+  int device = 0;
+  int N = 0;       // mesh side
+  int Ng = 0;      // contraction grid side
+  int n = 0;       // shells
+  int qmax = 0;    // largest |q_c| of a mode in any shell
+  double L = 0.0;
+  size_t mem_budget = 0;
+  int chunk = 0;   // shells per FFT batch
+  std::vector<double> edges;  // 2n
+  std::vector<int64_t> counts;
+  int64_t K = 0;        // Ng^3
+  int64_t Mh = 0;       // Ng*Ng*(Ng/2+1) half-complex modes
+  uint16_t* table = nullptr;  // device [Mh] shell code
+  double* d_edges = nullptr;  // device [2n]
+  cufftHandle r2c = 0;        // N^3 R2C
+  bool r2c_ok = false;
+  cufftHandle c2r = 0;        // Ng^3 C2R, batch = chunk
+  bool c2r_ok = false;
+  cufftHandle z2d = 0;        // Ng^3 Z2D, batch = chunk (grid info)
+  bool z2d_ok = false;
+  bsk::FieldSlot slot[3];
+  cufftComplex* chunk_spec = nullptr;   // [chunk][Mh] masked spectra
+  int num_sms = 0;
+  void* work = nullptr;                 // cuFFT work area shared by the plan's transforms
+  size_t work_bytes = 0;
+  int n_alloc() const { return (n + chunk - 1) / chunk * chunk; }  // shells rounded to batches
+};
+
+struct bsk_triset {
+  bsk_plan* plan = nullptr;
+  int64_t T = 0;
+  std::vector<bsk::HostTriangle> tri;
+  int max_shell = -1;
+  bsk::DeviceSchedule sched;
+  int2* dups = nullptr;  // device (dst, src): repeated triangles copy the first occurrence
+  int n_dups = 0;
+};
+
+namespace bsk {
+
+// ---------------------------------------------------------------- kernels
+// Shell table + exact mode counts (FP64 predicate, Hermitian weights).
+void launch_shell_table(const bsk_plan* p, unsigned long long* d_counts, int* d_flag,
+                        cudaStream_t st);
+// Copy the |q_c| < Ng/2 modes of an N^3 half spectrum into the Ng half grid,
+// scaled by 1/N^3.
+void launch_extract(const bsk_plan* p, const cufftComplex* fine, cufftComplex* coarse,
+                    cudaStream_t st);
+// Masked spectra of shells [s0, s0+ns) into out[ns][Mh].
+void launch_filter(const bsk_plan* p, const cufftComplex* spec, int s0, int ns,
+                   cufftComplex* out, cudaStream_t st);
+// Indicator (or |k|-weighted when kweight) spectra, complex128.
+void launch_filter_indicator(const bsk_plan* p, int s0, int ns, int kweight,
+                             cufftDoubleComplex* out, cudaStream_t st);
+// FP32 -> (bf16 hi, bf16 lo) split, n elements.
+void launch_split(const float* in, __nv_bfloat16* hi, __nv_bfloat16* lo, int64_t n,
+                  cudaStream_t st);
+
+// SIMT contraction (Tin = float|double input fields, Tacc = float|double tile sums).
+// out[t] += sum over K of f1[i] f2[j] f3[l]  (out must be zeroed by the caller).
+void launch_contract_simt_f32(const DeviceSchedule& s, const float* f1, const float* f2,
+                              const float* f3, int n_shells, int64_t K, int64_t k_begin,
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st);
+void launch_contract_simt_f64(const DeviceSchedule& s, const float* f1, const float* f2,
+                              const float* f3, int n_shells, int64_t K, int64_t k_begin,
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st);
+void launch_contract_simt_d64(const DeviceSchedule& s, const double* f1, const double* f2,
+                              const double* f3, int n_shells, int64_t K, int64_t k_begin,
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st);
+
+// tcgen05 contraction: f1/f2 FP32 (pair-product sources), f3 as bf16 hi/lo.
+void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f2,
+                        const __nv_bfloat16* f3_hi, const __nv_bfloat16* f3_lo, int n_shells,
+                        int64_t K, int64_t k_begin, int64_t k_end, int terms, double* out,
+                        int num_sms, cudaStream_t st);
+
+// Bounded-wait error flag of the tcgen05 kernel (1 = a wait expired); optionally reset.
+int tc_error_flag(bool reset);
+
+void launch_scale(double* v, int64_t n, double s, cudaStream_t st);
+void launch_gridinfo_finish(int64_t T, double inv_k, double* ntri, const double* s1,
+                            const double* s2, const double* s3, double* kmean,
+                            cudaStream_t st);
+void launch_normalize(int64_t n, const double* b, const double* ntri, double* out,
+                      cudaStream_t st);
+
+}  // namespace bsk

@@ -1,0 +1,165 @@
+// Host-side tile schedule for the triple-product contraction.
+//
+// B[t] = sum_x F1[i_t](x) F2[j_t](x) F3[l_t](x) is evaluated as a GEMM
+//   C[(i,j), l] = sum_x (F1[i] * F2[j])(x) * F3[l](x)
+// restricted to the (pair, l) entries that are triangle bins.  Every distinct
+// (i, j) pair is one GEMM row; rows are sorted by the range of third shells
+// they need and packed 128 to a tile, each tile covering a contiguous column
+// range [l0, l0 + nc).  The map [c][r] -> t scatters tile entries back to
+// triangle bins (-1 for entries that are not bins).
+#include <algorithm>
+#include <map>
+
+#include "bsk_internal.cuh"
+
+namespace bsk {
+
+void DeviceSchedule::release() {
+  if (tiles) cudaFree(tiles);
+  if (row_i) cudaFree(row_i);
+  if (row_j) cudaFree(row_j);
+  if (map) cudaFree(map);
+  if (subs) cudaFree(subs);
+  subs = nullptr;
+  n_sub = 0;
+  tiles = nullptr;
+  row_i = row_j = nullptr;
+  map = nullptr;
+  n_tiles = 0;
+  sum_nc = 0;
+  h_tiles.clear();
+}
+
+namespace {
+struct Row {
+  int i, j;
+  int lmin, lmax;
+  std::vector<std::pair<int, int>> cols;  // (l, t)
+};
+
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+}  // namespace
+
+void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSchedule& out) {
+  out.release();
+  std::map<std::pair<int, int>, int> index;
+  std::vector<Row> rows;
+  for (size_t t = 0; t < tri.size(); ++t) {
+    const HostTriangle& h = tri[t];
+    BSK_REQUIRE(h.i >= 0 && h.j >= 0 && h.l >= 0 && h.i < n_shells && h.j < n_shells &&
+                    h.l < n_shells,
+                BSK_ERR_ARG, "triangle shell index out of range");
+    auto key = std::make_pair(h.i, h.j);
+    auto it = index.find(key);
+    int r;
+    if (it == index.end()) {
+      r = (int)rows.size();
+      index.emplace(key, r);
+      rows.push_back(Row{h.i, h.j, h.l, h.l, {}});
+    } else {
+      r = it->second;
+    }
+    Row& R = rows[r];
+    R.lmin = std::min(R.lmin, h.l);
+    R.lmax = std::max(R.lmax, h.l);
+    R.cols.emplace_back(h.l, (int)t);
+  }
+  std::sort(rows.begin(), rows.end(), [](const Row& a, const Row& b) {
+    if (a.lmax != b.lmax) return a.lmax < b.lmax;
+    if (a.lmin != b.lmin) return a.lmin < b.lmin;
+    if (a.j != b.j) return a.j < b.j;
+    return a.i < b.i;
+  });
+
+  // Greedy packing under the tile constraints.
+  std::vector<std::vector<int>> groups;
+  {
+    std::vector<int> cur;
+    int lmin = 0, lmax = 0, imin = 0, imax = 0, jmin = 0, jmax = 0;
+    for (int r = 0; r < (int)rows.size(); ++r) {
+      const Row& R = rows[r];
+      if (!cur.empty()) {
+        int nl = std::min(lmin, R.lmin), xl = std::max(lmax, R.lmax);
+        int ni = std::min(imin, R.i), xi = std::max(imax, R.i);
+        int nj = std::min(jmin, R.j), xj = std::max(jmax, R.j);
+        bool fits = (int)cur.size() < kTileRows && round_up(xl - nl + 1, 16) <= kMaxCols &&
+                    round_up(xi - ni + 1, 8) <= kMaxSrcRows &&
+                    round_up(xj - nj + 1, 8) <= kMaxSrcRows;
+        if (fits) {
+          cur.push_back(r);
+          lmin = nl; lmax = xl; imin = ni; imax = xi; jmin = nj; jmax = xj;
+          continue;
+        }
+        groups.push_back(cur);
+        cur.clear();
+      }
+      cur.push_back(r);
+      lmin = R.lmin; lmax = R.lmax; imin = imax = R.i; jmin = jmax = R.j;
+    }
+    if (!cur.empty()) groups.push_back(cur);
+  }
+
+  std::vector<TileDesc> tiles;
+  std::vector<int16_t> ri, rj;
+  std::vector<int32_t> map;
+  int sum_nc = 0;
+  for (auto& g : groups) {
+    TileDesc d{};
+    int lmin = 1 << 30, lmax = -1, imin = 1 << 30, imax = -1, jmin = 1 << 30, jmax = -1;
+    for (int r : g) {
+      lmin = std::min(lmin, rows[r].lmin); lmax = std::max(lmax, rows[r].lmax);
+      imin = std::min(imin, rows[r].i); imax = std::max(imax, rows[r].i);
+      jmin = std::min(jmin, rows[r].j); jmax = std::max(jmax, rows[r].j);
+    }
+    d.l0 = lmin;
+    const int lo_ij = std::min(imin, jmin), hi_ij = std::max(imax, jmax);
+    if (hi_ij - lo_ij < kMaxSrcRows) {  // one source range serves both pair factors
+      d.i0 = d.j0 = lo_ij;
+      d.ni = d.nj = round_up(hi_ij - lo_ij + 1, 8);
+    } else {
+      d.i0 = imin; d.j0 = jmin;
+      d.ni = round_up(imax - imin + 1, 8);
+      d.nj = round_up(jmax - jmin + 1, 8);
+    }
+    d.nc = std::max(16, round_up(lmax - lmin + 1, 16));
+    d.nrows = (int)g.size();
+    d.row_off = (int)ri.size();
+    d.map_off = (int)map.size();
+    sum_nc += d.nc;
+    ri.resize(ri.size() + kTileRows, (int16_t)-1);
+    rj.resize(rj.size() + kTileRows, (int16_t)-1);
+    map.resize(map.size() + (size_t)d.nc * kTileRows, -1);
+    for (int k = 0; k < (int)g.size(); ++k) {
+      const Row& R = rows[g[k]];
+      ri[d.row_off + k] = (int16_t)R.i;
+      rj[d.row_off + k] = (int16_t)R.j;
+      for (auto& c : R.cols) map[d.map_off + (size_t)(c.first - lmin) * kTileRows + k] = c.second;
+    }
+    tiles.push_back(d);
+  }
+  out.n_tiles = (int)tiles.size();
+  out.sum_nc = sum_nc;
+  out.h_tiles = tiles;
+  if (tiles.empty()) return;
+  BSK_CHECK_CUDA(cudaMalloc(&out.tiles, tiles.size() * sizeof(TileDesc)));
+  BSK_CHECK_CUDA(cudaMalloc(&out.row_i, ri.size() * sizeof(int16_t)));
+  BSK_CHECK_CUDA(cudaMalloc(&out.row_j, rj.size() * sizeof(int16_t)));
+  BSK_CHECK_CUDA(cudaMalloc(&out.map, map.size() * sizeof(int32_t)));
+  BSK_CHECK_CUDA(cudaMemcpy(out.tiles, tiles.data(), tiles.size() * sizeof(TileDesc),
+                            cudaMemcpyHostToDevice));
+  BSK_CHECK_CUDA(cudaMemcpy(out.row_i, ri.data(), ri.size() * sizeof(int16_t),
+                            cudaMemcpyHostToDevice));
+  BSK_CHECK_CUDA(cudaMemcpy(out.row_j, rj.data(), rj.size() * sizeof(int16_t),
+                            cudaMemcpyHostToDevice));
+  BSK_CHECK_CUDA(cudaMemcpy(out.map, map.data(), map.size() * sizeof(int32_t),
+                            cudaMemcpyHostToDevice));
+  std::vector<int2> subs;
+  for (int u = 0; u < (int)tiles.size(); ++u)
+    for (int c = 0; c < tiles[u].nc; c += 32) subs.push_back(make_int2(u, c));
+  out.n_sub = (int)subs.size();
+  BSK_CHECK_CUDA(cudaMalloc(&out.subs, subs.size() * sizeof(int2)));
+  BSK_CHECK_CUDA(cudaMemcpy(out.subs, subs.data(), subs.size() * sizeof(int2),
+                            cudaMemcpyHostToDevice));
+}
+
+}  // namespace bsk

@@ -1,0 +1,194 @@
+"""Thin object layer over the C ABI (plans, triangle sets, device buffers).
+
+Tensors are torch CUDA tensors; every call is enqueued on the current torch
+stream of the plan's device.  Nothing here computes on the CPU.
+"""
+import ctypes
+import weakref
+
+import numpy as np
+import torch
+
+from . import _lib
+
+GRID_MODES = {"reduced": _lib.GRID_REDUCED, "native": _lib.GRID_NATIVE}
+
+
+def _stream_ptr(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("bskit_gb300 computes on a CUDA device only (none is available)")
+
+
+class TriangleSet:
+    """A registered list of (i, j, l) shell-index triples (``k_indices`` rows)."""
+
+    def __init__(self, plan, tri):
+        tri = np.ascontiguousarray(np.asarray(tri, dtype=np.int32).reshape(-1, 3))
+        self.plan = plan
+        self.indices = tri
+        self.T = len(tri)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(plan.device):
+            _lib.call("bsk_triset_create", plan.handle, self.T,
+                      tri.ctypes.data if self.T else None, ctypes.byref(h))
+        self.handle = h
+        plan._sets.add(self)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            with torch.cuda.device(self.plan.device):
+                _lib.load().bsk_triset_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Plan:
+    """Engine state for one (Nmesh, BoxSize, shell list) on one device.
+
+    ``grid='reduced'`` contracts on the smallest FFT-friendly grid Ng > 3 q_max
+    (identical sums, see ``bsk_plan_create``); ``grid='native'`` uses Ng = Nmesh.
+    """
+
+    def __init__(self, nmesh, box_size, shell_edges, grid="reduced", mem_budget=0, device=None):
+        _require_cuda()
+        self._sets = weakref.WeakSet()
+        idx = None if device is None else torch.device(device).index
+        self.device = torch.device("cuda", torch.cuda.current_device() if idx is None else idx)
+        edges = np.ascontiguousarray(np.asarray(shell_edges, dtype=np.float64).reshape(-1, 2))
+        self.shell_edges = edges
+        self.nmesh = int(nmesh)
+        self.box_size = float(box_size)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.call("bsk_plan_create", self.nmesh, self.box_size, len(edges), edges.ctypes.data,
+                      GRID_MODES[grid], int(mem_budget), ctypes.byref(h))
+        self.handle = h
+        info = (ctypes.c_int64 * _lib.INFO_COUNT)()
+        _lib.call("bsk_plan_query", self.handle, info)
+        self.ngrid = int(info[_lib.INFO_NGRID])
+        self.qmax = int(info[_lib.INFO_QMAX])
+        self.n_shells = len(edges)
+
+    # ------------------------------------------------------------------ info
+    def footprint(self):
+        info = (ctypes.c_int64 * _lib.INFO_COUNT)()
+        _lib.call("bsk_plan_query", self.handle, info)
+        return int(info[_lib.INFO_FOOTPRINT])
+
+    def mode_counts(self):
+        out = np.zeros(self.n_shells, dtype=np.int64)
+        _lib.call("bsk_shell_mode_counts", self.handle, out.ctypes.data)
+        return out
+
+    def triangles(self, tri):
+        return TriangleSet(self, tri)
+
+    # ------------------------------------------------------------------ compute
+    def paint(self, slot, mesh, stream=None):
+        """r2c of a real N^3 float32 CUDA tensor into field slot 0/1/2."""
+        m = self._as_mesh(mesh)
+        with torch.cuda.device(self.device):
+            _lib.call("bsk_paint", self.handle, int(slot), ctypes.c_void_p(m.data_ptr()),
+                      _stream_ptr(stream))
+        return m
+
+    def measure_b(self, tset, slots=(0, 0, 0), precision="bf16x3", out=None, stream=None):
+        """Unnormalised bispectrum (float64 CUDA tensor of length T)."""
+        prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        if out is None:
+            out = torch.empty(tset.T, dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.call("bsk_measure_b", self.handle, tset.handle, int(slots[0]), int(slots[1]),
+                      int(slots[2]), prec, ctypes.c_void_p(out.data_ptr()), _stream_ptr(stream))
+        return out
+
+    def measure_b_range(self, tset, k_begin, k_end, slots=(0, 0, 0), precision="bf16x3",
+                        out=None, stream=None):
+        """Partial unnormalised B over contraction-grid points [k_begin, k_end)."""
+        prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        if out is None:
+            out = torch.empty(tset.T, dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.call("bsk_measure_b_range", self.handle, tset.handle, int(slots[0]),
+                      int(slots[1]), int(slots[2]), prec, int(k_begin), int(k_end),
+                      ctypes.c_void_p(out.data_ptr()), _stream_ptr(stream))
+        return out
+
+    def gridinfo(self, tset, stream=None):
+        """(N_tri (T,), k_mean (T, 3)) float64 CUDA tensors; k_mean NaN where N_tri == 0."""
+        ntri = torch.empty(tset.T, dtype=torch.float64, device=self.device)
+        kmean = torch.empty((tset.T, 3), dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.call("bsk_gridinfo", self.handle, tset.handle, ctypes.c_void_p(ntri.data_ptr()),
+                      ctypes.c_void_p(kmean.data_ptr()), _stream_ptr(stream))
+        return ntri, kmean
+
+    def contract(self, tset, f1, f2, f3, precision="bf16x3", stream=None):
+        """Raw contraction of caller fields ([n][K] float32 CUDA): sum_k f1 f2 f3."""
+        prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        fs = [f.contiguous() for f in (f1, f2, f3)]
+        for f in fs:
+            if f.dtype != torch.float32 or not f.is_cuda or f.shape[0] != self.n_shells:
+                raise ValueError("fields must be float32 CUDA tensors of shape (n_shells, K)")
+        K = fs[0][0].numel()
+        out = torch.empty(tset.T, dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.call("bsk_contract", self.handle, tset.handle, *[ctypes.c_void_p(f.data_ptr())
+                                                                  for f in fs],
+                      int(K), prec, ctypes.c_void_p(out.data_ptr()), _stream_ptr(stream))
+        return out
+
+    def field(self, slot, shell, stream=None):
+        """FP32 real-space field of one shell on the contraction grid (Ng^3)."""
+        out = torch.empty((self.ngrid,) * 3, dtype=torch.float32, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.call("bsk_copy_field", self.handle, int(slot), int(shell),
+                      ctypes.c_void_p(out.data_ptr()), _stream_ptr(stream))
+        return out
+
+    def sync_check(self, stream=None):
+        with torch.cuda.device(self.device):
+            _lib.call("bsk_sync_check", _stream_ptr(stream))
+
+    @staticmethod
+    def normalize(b_unnorm, ntri, stream=None):
+        out = torch.empty_like(b_unnorm)
+        _lib.call("bsk_normalize", int(b_unnorm.numel()), ctypes.c_void_p(b_unnorm.data_ptr()),
+                  ctypes.c_void_p(ntri.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                  _stream_ptr(stream))
+        return out
+
+    # ------------------------------------------------------------------ helpers
+    def _as_mesh(self, mesh):
+        if isinstance(mesh, np.ndarray):
+            mesh = torch.from_numpy(np.ascontiguousarray(mesh, dtype=np.float32))
+        if not isinstance(mesh, torch.Tensor):
+            raise TypeError("mesh must be a numpy array or torch tensor")
+        if tuple(mesh.shape) != (self.nmesh,) * 3:
+            raise ValueError("mesh shape %s does not match Nmesh=%d" % (tuple(mesh.shape),
+                                                                          self.nmesh))
+        return mesh.to(device=self.device, dtype=torch.float32).contiguous()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            for ts in list(self._sets):
+                ts.close()
+            with torch.cuda.device(self.device):
+                _lib.load().bsk_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,64 @@
+"""The C-ABI library loads without a GPU and exports every entry point of
+include/bskit_gb300.h with the signatures the ctypes binding declares."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from bskit_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "bskit_gb300.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t)\s+(bsk_\w+)\s*\(", src, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_lib.LIB_PATH):
+        from bskit_gb300 import build
+        build.build()
+    return _lib.load()
+
+
+def test_header_declares_the_boundary():
+    names = header_functions()
+    for required in ("bsk_plan_create", "bsk_paint", "bsk_measure_b", "bsk_gridinfo",
+                     "bsk_shell_mode_counts", "bsk_triset_create", "bsk_normalize"):
+        assert required in names
+
+
+def test_library_exports_every_header_symbol(lib):
+    for name in header_functions():
+        assert hasattr(lib, name), name
+
+
+def test_binding_covers_header(lib):
+    bound = {n for n, _, _ in _lib.SIGNATURES}
+    assert bound == set(header_functions())
+
+
+def test_version_and_error_text(lib):
+    assert lib.bsk_version() >= 100
+    # NULL out-pointer: rejected on the host before any CUDA call
+    rc = lib.bsk_plan_create(64, 100.0, 1, None, 0, 0, None)
+    assert rc == _lib.BSK_ERR_ARG
+    assert "NULL" in _lib.last_error()
+    assert lib.bsk_triset_size(None) == -1
+    buf = ctypes.create_string_buffer(4)
+    assert lib.bsk_last_error(buf, 4) == 0 and len(buf.value) <= 3
+
+
+def test_bad_arguments_rejected_without_gpu(lib):
+    out = ctypes.c_void_p()
+    edges = (ctypes.c_double * 2)(0.1, 0.2)
+    assert lib.bsk_plan_create(63, 100.0, 1, edges, 0, 0, ctypes.byref(out)) == _lib.BSK_ERR_ARG
+    assert lib.bsk_plan_create(64, -1.0, 1, edges, 0, 0, ctypes.byref(out)) == _lib.BSK_ERR_ARG
+    assert lib.bsk_plan_create(64, 100.0, 0, edges, 0, 0, ctypes.byref(out)) == _lib.BSK_ERR_ARG
+    assert lib.bsk_plan_create(64, 100.0, 1, edges, 7, 0, ctypes.byref(out)) == _lib.BSK_ERR_ARG
+    assert lib.bsk_normalize(-1, None, None, None, None) == _lib.BSK_ERR_ARG

@@ -1,0 +1,262 @@
+"""GPU path vs the FP64 oracle (and vs bskit's golden grid info), through the C ABI.
+
+Tolerances (stated per test):
+* shell mode counts and triangle counts: bit-exact integers;
+* k_mean: 1e-12 relative (FP64 fields and sums on both sides);
+* B: the GPU fields are FP32 (cuFFT C2R), the oracle's FP64.  For every bin we
+  report rel = |B - B_o| / |B_o| and the conditioning-free
+  nrm = |B - B_o| / (L^6/N^3 * sum_x |I_i I_j I_l|).  fp64/fp32/bf16x3 must meet
+  nrm <= 2e-6 everywhere and rel <= 1e-5 on bins with |B_o| >= 1e-2 of the
+  absolute sum; bf16 (one MMA term) must meet nrm <= 1e-2.
+"""
+import numpy as np
+import pytest
+import torch
+
+from bskit_gb300 import bins as B
+from bskit_gb300 import synthetic
+from bskit_gb300.engine import Plan
+from oracle import bispec_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TWO_PI = 2 * np.pi
+
+
+def _cfg0():
+    n, box = 64, 100.0
+    kf = TWO_PI / box
+    kw = dict(kmin=kf, kmax=16 * kf, dk=3 * kf)
+    return n, box, B.generate_bin_edge_list(**kw), B.generate_triangle_bin_list(return_indices=True, **kw)
+
+
+def _small(n=32, box=100.0, dk=2, kmax_frac=0.25):
+    kf = TWO_PI / box
+    kw = dict(kmin=kf, kmax=n * kmax_frac * kf, dk=dk * kf)
+    return n, box, B.generate_bin_edge_list(**kw), B.generate_triangle_bin_list(return_indices=True, **kw)
+
+
+def _abs_sums(fa, fb, fc, tri, box, n):
+    return O.triple_sums(np.abs(fa), np.abs(fb), np.abs(fc), tri) * box ** 6 / n ** 3
+
+
+def _check_b(b, bo, babs, prec):
+    err = np.abs(b - bo)
+    nrm = err / babs
+    rel = err / np.abs(bo)
+    well = np.abs(bo) >= 1e-2 * babs
+    print("%s: max nrm %.3g, max rel(well-conditioned, %d/%d bins) %.3g, median rel %.3g" %
+          (prec, nrm.max(), well.sum(), len(bo), rel[well].max() if well.any() else 0,
+           np.median(rel)))
+    if prec == "bf16":
+        assert nrm.max() <= 1e-2
+    else:
+        assert nrm.max() <= 2e-6
+        if well.any():
+            assert rel[well].max() <= 1e-5
+
+
+@pytest.mark.parametrize("grid", ["native", "reduced"])
+def test_mode_counts_exact(cuda, grid):
+    for n, box, edges, _ in (_cfg0(), _small(32, 100.0, 2), _small(48, 77.0, 1, 0.5)):
+        plan = Plan(n, box, edges, grid=grid)
+        assert np.array_equal(plan.mode_counts(), O.shell_mode_counts(n, box, edges))
+        plan.close()
+    # golden P(k) N_modes 18, 62, 98, 210 at L = 1000
+    kf = TWO_PI / 1000.0
+    edges = np.array([[0.5 + i, 1.5 + i] for i in range(4)]) * kf
+    plan = Plan(512, 1000.0, edges, grid="reduced")
+    assert plan.ngrid < 512
+    assert plan.mode_counts().tolist() == [18, 62, 98, 210]
+
+
+def test_gridinfo_matches_golden_text(cuda):
+    up = dict(kmin=0.00314, kmax=0.1, dk=0.00628, num_lowk_bins=3, dk_high=0.01884)
+    edges = B.generate_bin_edge_list(**up)
+    tri = B.generate_triangle_bin_list(return_indices=True, **up)
+    plan = Plan(512, 1000.0, edges, grid="reduced")  # the mesh size of the golden run
+    ts = plan.triangles(tri)
+    nt, km = plan.gridinfo(ts)
+    plan.sync_check()
+    nt, km = nt.cpu().numpy(), km.cpu().numpy()
+    ed6 = B.triangle_indices_to_edges(edges, tri)
+    rows = ['%d %e %e %e %e %e %e %e %e %e %e' % ((t,) + tuple(km[t]) + tuple(ed6[t]) + (nt[t],))
+            for t in range(len(tri))]
+    import os
+    gold = open(os.path.join(os.path.dirname(__file__), "golden",
+                             "Lbox1000_512_kf_3kf_3lowkbins.dat")).read().split("\n")[:len(rows)]
+    assert rows == gold
+
+
+@pytest.mark.parametrize("grid", ["native", "reduced"])
+def test_gridinfo_exact_vs_oracle(cuda, grid):
+    # edges at multiples of k_f: many modes sit exactly on shell edges
+    n, box, edges, tri = _small(32, 100.0, 2)
+    plan = Plan(n, box, edges, grid=grid)
+    ts = plan.triangles(tri)
+    nt, km = plan.gridinfo(ts)
+    plan.sync_check()
+    raw, nto, kmo = O.grid_info(n, box, edges, tri)
+    assert np.array_equal(nt.cpu().numpy(), nto)
+    km = km.cpu().numpy()
+    ok = nto > 0
+    assert np.all(np.isnan(km[~ok]))
+    assert np.allclose(km[ok], kmo[ok], rtol=1e-12, atol=0)
+
+
+def test_fields_match_oracle_native(cuda):
+    n, box, edges, _ = _small(32, 100.0, 2)
+    delta = synthetic.lognormal_mesh(n, box, seed=11)
+    plan = Plan(n, box, edges, grid="native")
+    plan.paint(0, torch.from_numpy(delta))
+    of = O.shell_fields(O.spectrum(delta), n, box, edges)
+    for s in range(len(edges)):
+        f = plan.field(0, s).cpu().numpy().astype(np.float64)
+        scale = np.abs(of[s]).max()
+        assert np.abs(f - of[s]).max() <= 1e-5 * scale, s
+
+
+def test_paint_keeps_input(cuda):
+    n, box, edges, _ = _small(32, 100.0, 2)
+    delta = torch.from_numpy(synthetic.lognormal_mesh(n, box, seed=12)).cuda()
+    keep = delta.clone()
+    plan = Plan(n, box, edges)
+    plan.paint(0, delta)
+    torch.cuda.synchronize()
+    assert torch.equal(delta, keep)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "bf16x3", "bf16"])
+def test_auto_bispectrum_cfg0(cuda, prec):
+    n, box, edges, tri = _cfg0()
+    delta = synthetic.lognormal_mesh(n, box, seed=0)
+    plan = Plan(n, box, edges, grid="reduced")
+    plan.paint(0, torch.from_numpy(delta))
+    ts = plan.triangles(tri)
+    b = plan.measure_b(ts, precision=prec)
+    plan.sync_check()
+    of = O.shell_fields(O.spectrum(delta), n, box, edges)
+    bo = O.triple_sums(of, of, of, tri) * box ** 6 / n ** 3
+    _check_b(b.cpu().numpy(), bo, _abs_sums(of, of, of, tri, box, n), prec)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "bf16x3"])
+def test_auto_bispectrum_more_shells(cuda, prec):
+    # 15 shells, 477 bins: several tensor-core tiles and column ranges
+    n, box, edges, tri = _small(64, 100.0, 2, 0.25)
+    delta = synthetic.lognormal_mesh(n, box, seed=4)
+    plan = Plan(n, box, edges)
+    plan.paint(0, torch.from_numpy(delta))
+    ts = plan.triangles(tri)
+    b = plan.measure_b(ts, precision=prec)
+    plan.sync_check()
+    of = O.shell_fields(O.spectrum(delta), n, box, edges)
+    bo = O.triple_sums(of, of, of, tri) * box ** 6 / n ** 3
+    _check_b(b.cpu().numpy(), bo, _abs_sums(of, of, of, tri, box, n), prec)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "bf16x3"])
+def test_cross_bispectra(cuda, prec):
+    n, box = 48, 100.0
+    kf = TWO_PI / box
+    kw = dict(kmin=kf, kmax=12 * kf, dk=2 * kf)
+    edges = B.generate_bin_edge_list(**kw)
+    d1 = synthetic.lognormal_mesh(n, box, seed=21)
+    d2 = synthetic.noisy_copy(d1, seed=22)
+    d3 = synthetic.lognormal_mesh(n, box, seed=23)
+    plan = Plan(n, box, edges)
+    for s, d in enumerate((d1, d2, d3)):
+        plan.paint(s, torch.from_numpy(d))
+    f = [O.shell_fields(O.spectrum(d), n, box, edges) for d in (d1, d2, d3)]
+    for nf, slots in ((2, (0, 0, 1)), (3, (0, 1, 2))):
+        tri = B.generate_triangle_bin_list(num_fields=nf, return_indices=True, **kw)
+        ts = plan.triangles(tri)
+        b = plan.measure_b(ts, slots=slots, precision=prec)
+        plan.sync_check()
+        fa, fb, fc = (f[0], f[0], f[1]) if nf == 2 else (f[0], f[1], f[2])
+        bo = O.triple_sums(fa, fb, fc, tri) * box ** 6 / n ** 3
+        _check_b(b.cpu().numpy(), bo, _abs_sums(fa, fb, fc, tri, box, n), prec)
+
+
+def test_reduced_grid_equals_native(cuda):
+    n, box, edges, tri = _small(64, 100.0, 2, 0.25)
+    delta = torch.from_numpy(synthetic.lognormal_mesh(n, box, seed=8))
+    out = {}
+    for grid in ("native", "reduced"):
+        plan = Plan(n, box, edges, grid=grid)
+        plan.paint(0, delta)
+        out[grid] = plan.measure_b(plan.triangles(tri), precision="fp64").cpu().numpy()
+        if grid == "reduced":
+            assert plan.ngrid < n
+    scale = np.abs(out["native"]).max()
+    assert np.abs(out["native"] - out["reduced"]).max() <= 1e-6 * scale
+
+
+def test_plane_wave_known_answer(cuda):
+    n, box = 32, TWO_PI
+    q = [np.array([3, 0, 0]), np.array([0, 2, 0]), np.array([-3, -2, 0])]
+    phi, A = [0.3, -1.1, 0.5], 0.7
+    x = np.arange(n) * box / n
+    X, Y, Z = np.meshgrid(x, x, x, indexing="ij")
+    delta = sum(A * np.cos(qa[0] * X + qa[1] * Y + qa[2] * Z + p) for qa, p in zip(q, phi))
+    shells = np.array([[1.9, 2.1], [2.9, 3.1], [3.5, 3.7]])
+    plan = Plan(n, box, shells)
+    plan.paint(0, torch.from_numpy(delta.astype(np.float32)))
+    ts = plan.triangles([[1, 0, 2]])
+    expect = box ** 6 * A ** 3 * np.cos(sum(phi)) / 4.0
+    for prec in ("fp64", "fp32", "bf16x3"):
+        b = plan.measure_b(ts, precision=prec).cpu().numpy()[0]
+        assert abs(b - expect) <= 1e-5 * abs(expect), prec
+
+
+def test_brute_force_known_answer(cuda):
+    n, box = 16, 50.0
+    kf = TWO_PI / box
+    delta = synthetic.lognormal_mesh(n, box, seed=3)
+    shells = np.array([[0.5, 2.5], [1.5, 3.5], [2.5, 4.5]]) * kf
+    plan = Plan(n, box, shells)
+    plan.paint(0, torch.from_numpy(delta))
+    tri = np.array([[2, 1, 1], [2, 1, 0], [1, 1, 1]])
+    ts = plan.triangles(tri)
+    nt, km = plan.gridinfo(ts)
+    b = plan.measure_b(ts, precision="fp64")
+    Bn = plan.normalize(b, nt).cpu().numpy()
+    nt = nt.cpu().numpy()
+    for t, (i, j, l) in enumerate(tri):
+        Bd, Nd, k1, k2, k3 = O.bk_binned(delta.astype(np.float64), box, shells[i], shells[j],
+                                         shells[l])
+        assert nt[t] == Nd
+        assert abs(Bn[t] - Bd.real) <= 1e-5 * abs(Bd.real)
+
+
+def test_duplicate_and_unordered_triangles(cuda):
+    n, box, edges, tri = _small(32, 100.0, 2)
+    delta = torch.from_numpy(synthetic.lognormal_mesh(n, box, seed=9))
+    plan = Plan(n, box, edges)
+    plan.paint(0, delta)
+    base = plan.measure_b(plan.triangles(tri), precision="fp64").cpu().numpy()
+    perm = tri[:, [2, 0, 1]]
+    dup = np.concatenate([tri[:5], tri[:5], perm[:5]])
+    b = plan.measure_b(plan.triangles(dup), precision="fp64").cpu().numpy()
+    assert np.allclose(b[:5], base[:5], rtol=1e-12)
+    assert np.allclose(b[5:10], base[:5], rtol=1e-12)
+    assert np.allclose(b[10:15], base[:5], rtol=1e-9)
+
+
+def test_slab_ranges_sum_to_whole(cuda):
+    n, box, edges, tri = _small(64, 100.0, 2, 0.25)
+    delta = torch.from_numpy(synthetic.lognormal_mesh(n, box, seed=10))
+    plan = Plan(n, box, edges)
+    plan.paint(0, delta)
+    ts = plan.triangles(tri)
+    K = plan.ngrid ** 3
+    slab = plan.ngrid ** 2
+    for prec in ("fp64", "bf16x3"):
+        whole = plan.measure_b(ts, precision=prec).cpu().numpy()
+        cut = (plan.ngrid // 3) * slab // 64 * 64
+        parts = [plan.measure_b_range(ts, 0, cut, precision=prec),
+                 plan.measure_b_range(ts, cut, K, precision=prec)]
+        tot = sum(p.cpu().numpy() for p in parts)
+        # a different slab cut changes only the FP32 accumulation order of the tensor path
+        tol = 1e-12 if prec == "fp64" else 1e-6
+        assert np.abs(tot - whole).max() <= tol * np.abs(whole).max(), prec
