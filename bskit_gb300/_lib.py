@@ -91,7 +91,13 @@ def last_error():
     return buf.value.decode(errors="replace")
 
 
+class BskArgumentError(BskError, ValueError):
+    """BSK_ERR_ARG: the cases bskit raises ValueError for."""
+
+
 def check(status):
+    if status == BSK_ERR_ARG:
+        raise BskArgumentError(status, last_error())
     if status != BSK_OK:
         raise BskError(status, last_error())
     return status

@@ -29,6 +29,7 @@ class DeviceGuard {
 
 template <typename F>
 int guarded(F&& f) {
+  cudaGetLastError();  // a failure left by an earlier call must not be reported by this one
   try {
     f();
     return BSK_OK;

@@ -9,7 +9,7 @@
 //     tiles of the column fields (SWIZZLE_128B, K-major: the UMMA B operand)
 //     and the FP32 tile(s) of the pair-factor shells (one 64-shell tile when a
 //     single range covers both factors of every row, as for auto spectra);
-//   * warps 6..13 (2 per TMEM lane quadrant, one 32-point half each) read the
+//   * warps 10..17 (2 per TMEM lane quadrant, one 32-point half each) read the
 //     row's F1_i, F2_j from SMEM, form P = F1_i*F2_j, split P = hi + lo (bf16,
 //     lo = bf16(fma(a, b, -hi))) and store them with tcgen05.st into a 4-stage
 //     TMEM A-operand ring (lane = GEMM row);
@@ -17,8 +17,9 @@
 //     hi*Bhi + hi*Blo + lo*Bhi (bf16x3) or hi*Bhi (bf16): M=128, N=nc, K=16 x 4.
 //     The tensor core's FP32 accumulate truncates, so an accumulator is only
 //     ever fed ACC_CHUNKS chunks (<= 24 MMAs) and then handed over;
-//   * warps 2..5 drain each finished accumulator with tcgen05.ld, add it into
-//     per-thread FP32 registers (round-to-nearest), and at the end of the slice
+//   * warps 2..9 (2 per lane quadrant, 32 columns each) drain each finished
+//     accumulator with tcgen05.ld, add it into per-thread FP32 registers
+//     (round-to-nearest), and at the end of the slice
 //     add the entries that are triangle bins into the FP64 output (atomics).
 // Every mbarrier wait is bounded (globaltimer); on expiry the kernel records
 // an error flag, stops issuing work, drains its own MMAs and frees TMEM.
@@ -31,14 +32,19 @@ namespace tc {
 
 constexpr int KCH = 64;                       // points per chunk
 constexpr int ACC_CHUNKS = 2;                 // chunks summed inside one TMEM accumulator
-constexpr int STAGES = 4;                     // SMEM ring
+// SMEM ring depth: a stage holds B hi / lo (16 KB) + one or two FP32 source tiles
+// (16 KB each); 6 stages with one source tile, 4 with two.
+template <bool kTwoSrc> struct Ring {
+  static constexpr int kStageBytes = 2 * (kMaxCols * 128) + (kTwoSrc ? 2 : 1) * (2 * kMaxSrcRows * 128);
+  static constexpr int kStages = kTwoSrc ? 4 : 6;
+};
+constexpr int STAGES = 6;                     // upper bound over both rings
 constexpr int A_STAGES = 4;                   // TMEM A-operand ring
 constexpr int NACC = 2;                       // TMEM accumulators
 constexpr int B_TILE = kMaxCols * 128;        // 8 KB: <= 64 rows x 64 bf16
 constexpr int A_HALF = kMaxSrcRows * 128;     // 8 KB: 64 rows x 32 fp32
 constexpr int A_TILE = 2 * A_HALF;            // 16 KB
-constexpr int STAGE_BYTES = 2 * B_TILE + 2 * A_TILE;  // 48 KB
-constexpr int NUM_WARPS = 14;
+constexpr int NUM_WARPS = 18;                 // producer, MMA, 8 drain, 8 A-operand
 constexpr int THREADS = NUM_WARPS * 32;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_COL = 0;               // accumulator b at 64 b
@@ -57,7 +63,10 @@ struct Bars {
   uint32_t tmem_base;
 };
 
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*bars*/ + 1024 /*align slack*/;
+template <bool kTwoSrc>
+constexpr int smem_bytes() {
+  return Ring<kTwoSrc>::kStages * Ring<kTwoSrc>::kStageBytes + 1024 /*bars*/ + 1024 /*align*/;
+}
 
 // Tensor maps of one launch: bf16 column fields with 16/32/64-row boxes, FP32 sources.
 struct Maps {
@@ -102,17 +111,29 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 // Bounded wait: false when the wait expired or another role already gave up.
+// mbarrier.try_wait suspends the thread in hardware for a while, so the loop
+// is cheap; the clock is read every 16 polls and global memory (the shared
+// error flag, the wall clock) only about every 2^20 cycles, so that no memory
+// round trip sits between a barrier's completion and the waiter seeing it.
 __device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   if (mbar_try(bar, parity)) return true;
-  const unsigned long long t0 = globaltimer();
+  long long c0 = clock64();
+  unsigned long long t0 = 0;
   while (true) {
 #pragma unroll 1
-    for (int i = 0; i < 32; ++i)
+    for (int i = 0; i < 16; ++i)
       if (mbar_try(bar, parity)) return true;
-    if (*(volatile int*)&g_tc_error) return false;
-    if (globaltimer() - t0 > kTimeoutNs) {
-      atomicExch(&g_tc_error, 1);
-      return false;
+    const long long c = clock64();
+    if (c - c0 > (1ll << 20)) {
+      c0 = c;
+      if (*(volatile int*)&g_tc_error) return false;
+      const unsigned long long t = globaltimer();
+      if (t0 == 0) {
+        t0 = t;
+      } else if (t - t0 > kTimeoutNs) {
+        atomicExch(&g_tc_error, 1);
+        return false;
+      }
     }
   }
 }
@@ -199,12 +220,16 @@ __device__ __forceinline__ void load_cols(uint32_t dst, const CUtensorMap* m16,
   }
 }
 
-__global__ void __maxnreg__(144)
+// 18 warps: 5 share one SM sub-partition, whose 16K registers allow 102 per thread.
+template <bool kTwoSrc>
+__global__ void __launch_bounds__(THREADS, 1)
     contract_tc_kernel(const __grid_constant__ Maps maps, const TileDesc* __restrict__ tiles,
                        const int16_t* __restrict__ row_i, const int16_t* __restrict__ row_j,
                        const int32_t* __restrict__ map, int n_tiles, int same_src,
                        int64_t k_begin, int64_t k_end, int64_t n_items, int terms,
                        double* __restrict__ out) {
+  constexpr int STAGES = Ring<kTwoSrc>::kStages;
+  constexpr int STAGE_BYTES = Ring<kTwoSrc>::kStageBytes;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
@@ -226,7 +251,7 @@ __global__ void __maxnreg__(144)
     }
     for (int b = 0; b < NACC; ++b) {
       mbar_init(&bars->accfull[b], 1);
-      mbar_init(&bars->accempty[b], 4);
+      mbar_init(&bars->accempty[b], 8);
     }
     mbar_init(&bars->done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -252,7 +277,7 @@ __global__ void __maxnreg__(144)
       for (int64_t item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
         const int64_t sl = item / n_tiles;
         const TileDesc td = tiles[item % n_tiles];
-        const bool one_src = same_src && td.i0 == td.j0;
+        const bool one_src = !kTwoSrc || (same_src && td.i0 == td.j0);
         const int64_t x_begin = k_begin + sl * SLICE;
         const int64_t x_end = min(k_end, x_begin + SLICE);
         const uint32_t bbytes = (uint32_t)((td.nc == 64 ? 64 : td.nc) * 128);
@@ -332,11 +357,12 @@ __global__ void __maxnreg__(144)
       tc_commit(&bars->done);
       mbar_wait(&bars->done, 0);
     }
-  } else if (warp < 6) {
+  } else if (warp < 10) {
     // ------------------------------------------------------------ accumulator drain
     const int qd = warp & 3;
+    const int c0 = ((warp - 2) >> 2) * 32;  // this warp's 32 accumulator columns
     const int r = qd * 32 + lane;
-    const uint32_t taddr = tmem + ((uint32_t)(qd * 32) << 16);
+    const uint32_t taddr = tmem + ((uint32_t)(qd * 32) << 16) + c0;
     uint32_t grp = 0;
     bool ok = true;
     for (int64_t item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
@@ -346,9 +372,9 @@ __global__ void __maxnreg__(144)
       const int64_t x_end = min(k_end, x_begin + SLICE);
       const int64_t nch = (x_end - x_begin + KCH - 1) / KCH;
       const int64_t ngrp = (nch + ACC_CHUNKS - 1) / ACC_CHUNKS;
-      float acc[kMaxCols];
+      float acc[32];
 #pragma unroll
-      for (int c = 0; c < kMaxCols; ++c) acc[c] = 0.f;
+      for (int c = 0; c < 32; ++c) acc[c] = 0.f;
       for (int64_t g = 0; g < ngrp; ++g, ++grp) {
         const uint32_t b = grp % NACC;
         if (!__all_sync(0xffffffffu, mbar_wait(&bars->accfull[b], (grp / NACC) & 1))) {
@@ -357,8 +383,8 @@ __global__ void __maxnreg__(144)
         }
         tc_fence_after();
 #pragma unroll
-        for (int cc = 0; cc < kMaxCols / 16; ++cc) {
-          if (cc * 16 < td.nc) {
+        for (int cc = 0; cc < 2; ++cc) {
+          if (c0 + cc * 16 < td.nc) {
             uint32_t v[16];
             tmem_ld16(taddr + ACC_COL + b * 64 + cc * 16, v);
 #pragma unroll
@@ -370,10 +396,10 @@ __global__ void __maxnreg__(144)
         if (lane == 0) mbar_arrive(&bars->accempty[b]);
       }
       if (!ok) break;
-      const int32_t* mp = map + td.map_off + r;
+      const int32_t* mp = map + td.map_off + c0 * kTileRows + r;
 #pragma unroll
-      for (int c = 0; c < kMaxCols; ++c) {
-        if (c < td.nc) {
+      for (int c = 0; c < 32; ++c) {
+        if (c0 + c < td.nc) {
           const int t = __ldg(mp + c * kTileRows);
           if (t >= 0) atomicAdd(out + t, (double)acc[c]);
         }
@@ -382,7 +408,7 @@ __global__ void __maxnreg__(144)
   } else {
     // ------------------------------------------------------------ A-operand producers
     const int qd = warp & 3;
-    const int half = (warp - 6) >> 2;
+    const int half = (warp - 10) >> 2;
     const int r = qd * 32 + lane;
     const uint32_t tlane = (uint32_t)(qd * 32) << 16;
     uint32_t chunk = 0;
@@ -390,7 +416,7 @@ __global__ void __maxnreg__(144)
     for (int64_t item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
       const int64_t sl = item / n_tiles;
       const TileDesc td = tiles[item % n_tiles];
-      const bool one_src = same_src && td.i0 == td.j0;
+      const bool one_src = !kTwoSrc || (same_src && td.i0 == td.j0);
       const int64_t x_begin = k_begin + sl * SLICE;
       const int64_t x_end = min(k_end, x_begin + SLICE);
       const int ri = row_i[td.row_off + r];
@@ -514,18 +540,20 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
   tc::make_map(&m.lo64, BF, 2, f3_lo, K, n_shells, 64, 64);
   tc::make_map(&m.f1, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, f1, K, n_shells, 32, 64);
   tc::make_map(&m.f2, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, f2, K, n_shells, 32, 64);
-  static bool attr_set = false;
-  if (!attr_set) {
-    BSK_CHECK_CUDA(cudaFuncSetAttribute(tc::contract_tc_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        tc::SMEM_BYTES));
-    attr_set = true;
+  bool two_src = f1 != f2;
+  for (const TileDesc& d : s.h_tiles) two_src = two_src || d.i0 != d.j0;
+  static bool attr_set[2] = {false, false};
+  auto kern = two_src ? tc::contract_tc_kernel<true> : tc::contract_tc_kernel<false>;
+  const int smem = two_src ? tc::smem_bytes<true>() : tc::smem_bytes<false>();
+  if (!attr_set[two_src]) {
+    BSK_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr_set[two_src] = true;
   }
   const int64_t n_slices = (k_end - k_begin + tc::SLICE - 1) / tc::SLICE;
   const int64_t n_items = n_slices * s.n_tiles;
   int64_t grid = num_sms;
   if (grid > n_items) grid = n_items;
-  tc::contract_tc_kernel<<<(unsigned)grid, tc::THREADS, tc::SMEM_BYTES, st>>>(
+  kern<<<(unsigned)grid, tc::THREADS, smem, st>>>(
       m, s.tiles, s.row_i, s.row_j, s.map, s.n_tiles, f1 == f2 ? 1 : 0, k_begin, k_end,
       n_items, terms, out);
   BSK_CHECK_CUDA(cudaGetLastError());

@@ -6,8 +6,10 @@ Tolerances (stated per test):
 * B: the GPU fields are FP32 (cuFFT C2R), the oracle's FP64.  For every bin we
   report rel = |B - B_o| / |B_o| and the conditioning-free
   nrm = |B - B_o| / (L^6/N^3 * sum_x |I_i I_j I_l|).  fp64/fp32/bf16x3 must meet
-  nrm <= 2e-6 everywhere and rel <= 1e-5 on bins with |B_o| >= 1e-2 of the
-  absolute sum; bf16 (one MMA term) must meet nrm <= 1e-2.
+  nrm <= 2e-6 on every bin, rel <= 1e-5 on every bin whose value is at least 10%
+  of its absolute sum (|B_o| >= 0.1 * abs sum; below that a 1e-6 normalised error
+  is no longer a 1e-5 relative one), and a median rel <= 1e-5 over all bins;
+  bf16 (one MMA term) must meet nrm <= 1e-3.
 """
 import numpy as np
 import pytest
@@ -44,14 +46,15 @@ def _check_b(b, bo, babs, prec):
     err = np.abs(b - bo)
     nrm = err / babs
     rel = err / np.abs(bo)
-    well = np.abs(bo) >= 1e-2 * babs
+    well = np.abs(bo) >= 0.1 * babs
     print("%s: max nrm %.3g, max rel(well-conditioned, %d/%d bins) %.3g, median rel %.3g" %
           (prec, nrm.max(), well.sum(), len(bo), rel[well].max() if well.any() else 0,
            np.median(rel)))
     if prec == "bf16":
-        assert nrm.max() <= 1e-2
+        assert nrm.max() <= 1e-3
     else:
         assert nrm.max() <= 2e-6
+        assert np.median(rel) <= 1e-5
         if well.any():
             assert rel[well].max() <= 1e-5
 
