@@ -42,6 +42,15 @@ def parse():
     ap.add_argument("--precision", default="bf16x3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=200,
+                    help="requests of the serving leg (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=40.0, help="Poisson arrival rate, req/s")
+    ap.add_argument("--serve-full", action="store_true",
+                    help="serving mix with N=512 (10%%) as well; default mix is N in 64/128/256")
+    ap.add_argument("--serve-only", action="store_true", help="run only the serving leg")
+    ap.add_argument("--no-cold", action="store_true",
+                    help="profiling runs only: skip the one-off FP64 grid information and "
+                         "normalise by 1 (same kernels and timings in the step)")
     return ap.parse_args()
 
 
@@ -161,9 +170,13 @@ def run_ours(args):
 
     # ---- cold: grid information (FP64), once
     t0 = time.perf_counter()
-    ntri, kmean = plan.gridinfo(ts)
-    plan.sync_check()
-    cold_gridinfo_s = time.perf_counter() - t0
+    if args.no_cold:
+        ntri = torch.ones(len(tri), dtype=torch.float64, device=dev)
+        cold_gridinfo_s = None
+    else:
+        ntri, kmean = plan.gridinfo(ts)
+        plan.sync_check()
+        cold_gridinfo_s = time.perf_counter() - t0
 
     stream = torch.cuda.current_stream()
     prec = args.precision
@@ -258,6 +271,7 @@ def run_ours(args):
         from oracle.cpu_baseline import ReferenceCPU
         ref = ReferenceCPU(delta.cpu().numpy(), BOX, edges, tri)
         try:
+            ref.step()  # warm-up (page faults, worker start)
             est = ref.step()
             cpu = {"value": 1.0 / est, "unit": "bispectra/s", "cores": ref.P, "kind": "port",
                    "sample": ref.describe(), "sample_seconds": ref.last["sample_seconds"]}
@@ -300,10 +314,78 @@ def run_ours(args):
     }
     if fp32:
         line["speedup_vs_fp32_plain"] = value / fp32["value"]
+    if args.serve_requests > 0 and world == 1:
+        plan.close()
+        del delta, host, dmesh
+        torch.cuda.empty_cache()
+        line["serving"] = run_serving(args, dev)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_serving(args, dev):
+    """Continuous-batching leg: seeded Poisson stream of mixed bispectrum requests.
+
+    Mix: N in {64,128,256,512} with weights {.4,.3,.2,.1} (512 only with
+    --serve-full; otherwise the first three, renormalised), 30% cross <AAB>,
+    bin set uniform over {all triangles dk=2kf to kNyq/2, equilateral, squeezed
+    with k1 in [kf, 3kf] (index 0)}, L = 100 Mpc/h, lognormal meshes (a seeded
+    pool per N), bf16x3.  Every configuration is served once before the timed
+    stream (plans, graphs and grid information resident); latency = arrival to
+    result on the host.
+    """
+    import numpy as np
+    import torch
+
+    from bskit_gb300 import serving, synthetic
+    rng = np.random.default_rng(2024)
+    sizes = [64, 128, 256, 512] if args.serve_full else [64, 128, 256]
+    w = np.array([0.4, 0.3, 0.2, 0.1][:len(sizes)])
+    w = w / w.sum()
+    box = 100.0
+    kf = 2 * np.pi / box
+    pool = {}
+    for n in sizes:
+        k = {64: 8, 128: 8, 256: 4, 512: 2}[n]
+        pool[n] = [synthetic.lognormal_mesh_torch(n, box, seed=1000 * n + i, device=dev)
+                   .cpu().pin_memory() for i in range(k)]
+    torch.cuda.synchronize()
+    sets = ["all", "equilateral", "squeezed"]
+
+    def make(i, t):
+        n = int(rng.choice(sizes, p=w))
+        kind = sets[int(rng.integers(3))]
+        cross = rng.random() < 0.3
+        spec = dict(kmin=kf, kmax=n / 4 * kf, dk=2 * kf, triangle_type=kind,
+                    squeezed_bin_index=0)
+        p = pool[n]
+        second = p[(i + 1) % len(p)] if cross else None
+        return serving.Request(i, p[i % len(p)], box, spec, second=second, arrival=t)
+
+    server = serving.make_server(max_batch=4, device=dev)
+    warm = []
+    for n in sizes:
+        for kind in sets:
+            for cross in (False, True):
+                spec = dict(kmin=kf, kmax=n / 4 * kf, dk=2 * kf, triangle_type=kind,
+                            squeezed_bin_index=0)
+                warm.append(serving.Request(-1, pool[n][0], box, spec,
+                                            second=pool[n][1] if cross else None))
+    t0 = time.perf_counter()
+    server.run(warm, realtime=False)
+    warm_s = time.perf_counter() - t0
+    server.done = []
+    gaps = rng.exponential(1.0 / args.serve_rate, size=args.serve_requests)
+    reqs = [make(i, t) for i, t in enumerate(np.cumsum(gaps))]
+    server.run(reqs, realtime=True)
+    stats = serving.latency_stats(reqs)
+    stats.update({"rate_rps": args.serve_rate, "mix": "N %s, weights %s, 30%% cross, "
+                  "all/equilateral/squeezed" % (sizes, [round(x, 3) for x in w]),
+                  "warmup_s": warm_s, "precision": "bf16x3", "max_batch": 4,
+                  "resident_groups": len(server.groups)})
+    return stats
 
 
 def run_reference(args):
@@ -348,6 +430,11 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.serve_only:
+        import torch
+        torch.cuda.set_device(0)
+        stats = run_serving(args, torch.device("cuda", 0))
+        print(json.dumps({"metric": "serve p50/p99 latency", "unit": "ms", "serving": stats}))
     else:
         run_ours(args)
 

@@ -47,6 +47,7 @@ SIGNATURES = [
     ("bsk_triset_destroy", _INT, [_VP]),
     ("bsk_triset_size", _I64, [_VP]),
     ("bsk_paint", _INT, [_VP, _INT, _VP, _VP]),
+    ("bsk_paint_cic", _INT, [_VP, _INT, _VP, _INT, _VP]),
     ("bsk_measure_b", _INT, [_VP, _VP, _INT, _INT, _INT, _INT, _VP, _VP]),
     ("bsk_measure_b_range", _INT, [_VP, _VP, _INT, _INT, _INT, _INT, _I64, _I64, _VP, _VP]),
     ("bsk_gridinfo", _INT, [_VP, _VP, _VP, _VP, _VP]),

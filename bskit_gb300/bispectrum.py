@@ -51,7 +51,8 @@ class FFTBispectrum(object):
         triple-product contraction of B (grid information always uses FP64);
     grid : 'reduced' (default) or 'native' -- see ``engine.Plan``;
     device : CUDA device of the computation;
-    mem_budget : bytes of shell fields the engine may keep resident (0 = no limit).
+    mem_budget : bytes of device memory the engine plan may hold (0 = no limit); a
+        measurement that would exceed it raises BskError (BSK_ERR_OOM) before allocating.
     """
     logger = logging.getLogger('FFTBispectrum')
 
@@ -175,7 +176,7 @@ class FFTBispectrum(object):
     def _paint_plan(self, plan):
         if not plan.painted:
             for s, m in enumerate(self._meshes()):
-                plan.paint(s, m.tensor(plan.device))
+                plan.paint(s, m.tensor(plan.device), cic_nmesh=m.compensate_cic)
             plan.painted = True
 
     def _paint_meshes(self):

@@ -128,11 +128,36 @@ void bind_work(bsk_plan* p, cufftHandle h, cudaStream_t st) {
 }
 
 // Masked shell fields of `slot` for every shell: filter kernel + batched C2R.
+// Device bytes the plan holds: shell table, filter staging, per-slot spectra,
+// fields and bf16 splits, and the shared cuFFT work area.
+int64_t footprint(const bsk_plan* p) {
+  int64_t fp = (int64_t)p->Mh * 2 + (int64_t)p->chunk * p->Mh * 8;
+  for (const auto& s : p->slot) {
+    if (s.spec) fp += p->Mh * 8;
+    if (s.fields) fp += (int64_t)p->n_alloc() * p->K * 4;
+    if (s.hi) fp += (int64_t)p->n_alloc() * p->K * 4;
+  }
+  return fp + (int64_t)p->work_bytes;
+}
+
+// Refuse an allocation of `bytes` that would take the plan above its budget.
+void check_budget(const bsk_plan* p, size_t bytes, const char* what) {
+  if (p->mem_budget == 0) return;
+  const int64_t after = footprint(p) + (int64_t)bytes;
+  if (after > (int64_t)p->mem_budget)
+    throw Error{BSK_ERR_OOM, std::string(what) + " would take the plan to " +
+                                 std::to_string(after) + " bytes, above its budget of " +
+                                 std::to_string(p->mem_budget)};
+}
+
 void ensure_fields(bsk_plan* p, int s, cudaStream_t st) {
   FieldSlot& f = p->slot[s];
   BSK_REQUIRE(f.painted, BSK_ERR_STATE, "field slot " + std::to_string(s) + " was not painted");
   if (f.fields_ok) return;
-  if (!f.fields) f.fields = (float*)dmalloc((size_t)p->n_alloc() * p->K * sizeof(float));
+  if (!f.fields) {
+    check_budget(p, (size_t)p->n_alloc() * p->K * sizeof(float), "the shell fields");
+    f.fields = (float*)dmalloc((size_t)p->n_alloc() * p->K * sizeof(float));
+  }
   bind_work(p, p->c2r, st);
   for (int s0 = 0; s0 < p->n; s0 += p->chunk) {
     int ns = std::min(p->chunk, p->n - s0);
@@ -152,6 +177,7 @@ void ensure_split(bsk_plan* p, int s, cudaStream_t st) {
   ensure_fields(p, s, st);
   if (f.split_ok) return;
   size_t n = (size_t)p->n_alloc() * p->K;
+  if (!f.hi) check_budget(p, n * 2 * sizeof(__nv_bfloat16), "the bf16 split of the fields");
   if (!f.hi) f.hi = (__nv_bfloat16*)dmalloc(n * sizeof(__nv_bfloat16));
   if (!f.lo) f.lo = (__nv_bfloat16*)dmalloc(n * sizeof(__nv_bfloat16));
   launch_split(f.fields, f.hi, f.lo, (int64_t)n, st);
@@ -174,6 +200,7 @@ void destroy_plan(bsk_plan* p) {
   if (p->table) cudaFree(p->table);
   if (p->d_edges) cudaFree(p->d_edges);
   if (p->chunk_spec) cudaFree(p->chunk_spec);
+  if (p->cic_w) cudaFree(p->cic_w);
   if (p->r2c_ok) cufftDestroy(p->r2c);
   if (p->c2r_ok) cufftDestroy(p->c2r);
   if (p->z2d_ok) cufftDestroy(p->z2d);
@@ -335,13 +362,7 @@ int bsk_plan_destroy(bsk_plan* plan) {
 int bsk_plan_query(const bsk_plan* p, int64_t* info) {
   return guarded([&] {
     BSK_REQUIRE(p && info, BSK_ERR_ARG, "NULL argument");
-    int64_t fp = (int64_t)p->Mh * 2 + (int64_t)p->chunk * p->Mh * 8;
-    for (const auto& s : p->slot) {
-      if (s.spec) fp += p->Mh * 8;
-      if (s.fields) fp += (int64_t)p->n_alloc() * p->K * 4;
-      if (s.hi) fp += (int64_t)p->n_alloc() * p->K * 4;
-    }
-    fp += (int64_t)p->work_bytes;
+    const int64_t fp = footprint(p);
     info[BSK_INFO_NMESH] = p->N;
     info[BSK_INFO_NGRID] = p->Ng;
     info[BSK_INFO_NSHELLS] = p->n;
@@ -438,23 +459,61 @@ int bsk_triset_destroy(bsk_triset* set) {
 
 int64_t bsk_triset_size(const bsk_triset* set) { return set ? set->T : -1; }
 
+namespace bsk {
+namespace {
+// Factors 1/sqrt(1 - 2/3 sin^2(pi q / NmeshCIC)) for q = -N/2..N/2, the per-axis CIC
+// window deconvolution of the mesh's source grid.
+void ensure_cic_table(bsk_plan* p, int nmesh_cic) {
+  if (p->cic_w && p->cic_nmesh == nmesh_cic) return;
+  std::vector<float> w(p->N + 1);
+  for (int i = 0; i <= p->N; ++i) {
+    const int q = i - p->N / 2;
+    const double s = std::sin(3.14159265358979323846 * q / nmesh_cic);
+    w[i] = (float)(1.0 / std::sqrt(1.0 - 2.0 / 3.0 * s * s));
+  }
+  if (!p->cic_w) p->cic_w = (float*)dmalloc(w.size() * sizeof(float));
+  BSK_CHECK_CUDA(cudaMemcpy(p->cic_w, w.data(), w.size() * sizeof(float),
+                            cudaMemcpyHostToDevice));
+  p->cic_nmesh = nmesh_cic;
+}
+
+void paint(bsk_plan* p, int slot, const float* mesh, int nmesh_cic, cudaStream_t st) {
+  BSK_REQUIRE(p && mesh, BSK_ERR_ARG, "NULL argument");
+  BSK_REQUIRE(slot >= 0 && slot < 3, BSK_ERR_ARG, "slot must be 0, 1 or 2");
+  FieldSlot& f = p->slot[slot];
+  const float* axis_w = nullptr;
+  if (nmesh_cic > 0) {
+    ensure_cic_table(p, nmesh_cic);
+    axis_w = p->cic_w;
+  }
+  size_t fine_elems = (size_t)p->N * p->N * (p->N / 2 + 1);
+  cufftComplex* fine = (cufftComplex*)dmalloc_async(fine_elems * sizeof(cufftComplex), st);
+  bind_work(p, p->r2c, st);
+  BSK_CHECK_CUFFT(cufftExecR2C(p->r2c, const_cast<float*>(mesh), fine));
+  if (!f.spec) f.spec = (cufftComplex*)dmalloc((size_t)p->Mh * sizeof(cufftComplex));
+  launch_extract(p, fine, f.spec, axis_w, st);
+  BSK_CHECK_CUDA(cudaFreeAsync(fine, st));
+  f.painted = true;
+  f.fields_ok = false;
+  f.split_ok = false;
+}
+}  // namespace
+}  // namespace bsk
+
 int bsk_paint(bsk_plan* p, int slot, const float* mesh, void* stream) {
   return guarded([&] {
-    BSK_REQUIRE(p && mesh, BSK_ERR_ARG, "NULL argument");
-    BSK_REQUIRE(slot >= 0 && slot < 3, BSK_ERR_ARG, "slot must be 0, 1 or 2");
+    BSK_REQUIRE(p, BSK_ERR_ARG, "NULL plan");
     DeviceGuard g(p->device);
-    cudaStream_t st = (cudaStream_t)stream;
-    FieldSlot& f = p->slot[slot];
-    size_t fine_elems = (size_t)p->N * p->N * (p->N / 2 + 1);
-    cufftComplex* fine = (cufftComplex*)dmalloc_async(fine_elems * sizeof(cufftComplex), st);
-    bind_work(p, p->r2c, st);
-    BSK_CHECK_CUFFT(cufftExecR2C(p->r2c, const_cast<float*>(mesh), fine));
-    if (!f.spec) f.spec = (cufftComplex*)dmalloc((size_t)p->Mh * sizeof(cufftComplex));
-    launch_extract(p, fine, f.spec, st);
-    BSK_CHECK_CUDA(cudaFreeAsync(fine, st));
-    f.painted = true;
-    f.fields_ok = false;
-    f.split_ok = false;
+    paint(p, slot, mesh, 0, (cudaStream_t)stream);
+  });
+}
+
+int bsk_paint_cic(bsk_plan* p, int slot, const float* mesh, int nmesh_cic, void* stream) {
+  return guarded([&] {
+    BSK_REQUIRE(p, BSK_ERR_ARG, "NULL plan");
+    BSK_REQUIRE(nmesh_cic > 0, BSK_ERR_ARG, "NmeshCIC must be positive");
+    DeviceGuard g(p->device);
+    paint(p, slot, mesh, nmesh_cic, (cudaStream_t)stream);
   });
 }
 
@@ -509,6 +568,8 @@ int bsk_gridinfo(bsk_plan* p, const bsk_triset* set, double* ntri, double* kmean
     make_z2d(p);
     bind_work(p, p->z2d, st);
     const size_t fbytes = (size_t)p->n_alloc() * p->K * sizeof(double);
+    check_budget(p, 2 * fbytes + (size_t)p->chunk * p->Mh * sizeof(cufftDoubleComplex),
+                 "the FP64 counting fields of the grid information");
     double* nf = (double*)dmalloc_async(fbytes, st);
     double* kf = (double*)dmalloc_async(fbytes, st);
     cufftDoubleComplex* spec = (cufftDoubleComplex*)dmalloc_async(

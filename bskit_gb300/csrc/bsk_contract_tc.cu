@@ -5,24 +5,29 @@
 // One persistent CTA per SM walks work items (tile of 128 pair rows x nc <= 64
 // columns, K slice of SLICE points), slice-major so that the CTAs running at
 // the same time share field data in L2.  Per 64-point chunk:
-//   * warp 0 (one lane) TMA-loads into a 4-stage SMEM ring the bf16 hi / lo
-//     tiles of the column fields (SWIZZLE_128B, K-major: the UMMA B operand)
-//     and the FP32 tile(s) of the pair-factor shells (one 64-shell tile when a
-//     single range covers both factors of every row, as for auto spectra);
+//   * warp 0 (one lane) TMA-loads into a 4-stage SMEM ring the bf16 hi and lo
+//     tiles of the column fields as one 128-row operand (rows 0..63 hi, 64..127
+//     lo; SWIZZLE_128B, K-major) and the FP32 tile(s) of the pair-factor shells
+//     (one 64-shell tile when one range covers both factors of every row, as for
+//     auto spectra);
 //   * warps 10..17 (2 per TMEM lane quadrant, one 32-point half each) read the
-//     row's F1_i, F2_j from SMEM, form P = F1_i*F2_j, split P = hi + lo (bf16,
-//     lo = bf16(fma(a, b, -hi))) and store them with tcgen05.st into a 4-stage
-//     TMEM A-operand ring (lane = GEMM row);
-//   * warp 1 (one lane) issues tcgen05.mma kind::f16 (A from TMEM, B from SMEM)
-//     hi*Bhi + hi*Blo + lo*Bhi (bf16x3) or hi*Bhi (bf16): M=128, N=nc, K=16 x 4.
-//     The tensor core's FP32 accumulate truncates, so an accumulator is only
-//     ever fed ACC_CHUNKS chunks (<= 24 MMAs) and then handed over;
+//     row's F1_i, F2_j from SMEM, form P = F1_i*F2_j with packed f32x2
+//     arithmetic, split P = hi + lo (bf16 round-to-nearest) and store them with
+//     tcgen05.st into the TMEM A-operand ring (lane = GEMM row);
+//   * warp 1 (one lane) issues, per 16-point K step, tcgen05.mma kind::f16 with
+//     A from TMEM and B from SMEM: hi x [Bhi; Blo] (N = 64 + nc: one MMA yields
+//     both hi*Bhi and hi*Blo) and, for bf16x3, lo x Bhi (N = nc).  The tensor
+//     core's FP32 accumulate truncates, so an accumulator is only ever fed
+//     ACC_CHUNKS chunks (16 MMAs) before it is handed over;
 //   * warps 2..9 (2 per lane quadrant, 32 columns each) drain each finished
-//     accumulator with tcgen05.ld, add it into per-thread FP32 registers
-//     (round-to-nearest), and at the end of the slice
-//     add the entries that are triangle bins into the FP64 output (atomics).
-// Every mbarrier wait is bounded (globaltimer); on expiry the kernel records
-// an error flag, stops issuing work, drains its own MMAs and frees TMEM.
+//     accumulator with tcgen05.ld (hi*B + lo*Bhi columns and hi*Blo columns),
+//     add it into per-thread FP32 registers (round-to-nearest), and at the end
+//     of the slice add the entries that are triangle bins into the FP64 output
+//     (atomics).
+// One mbarrier per stage carries the MMAs' completion back to both the TMA
+// producer (SMEM stage free) and the A-operand warps (TMEM stage free).  Every
+// wait is bounded (globaltimer); on expiry the kernel records an error flag,
+// stops issuing work, drains its own MMAs and frees TMEM.
 #include <cuda.h>
 
 #include "bsk_internal.cuh"
@@ -32,31 +37,28 @@ namespace tc {
 
 constexpr int KCH = 64;                       // points per chunk
 constexpr int ACC_CHUNKS = 2;                 // chunks summed inside one TMEM accumulator
-// SMEM ring depth: a stage holds B hi / lo (16 KB) + one or two FP32 source tiles
-// (16 KB each); 6 stages with one source tile, 4 with two.
-template <bool kTwoSrc> struct Ring {
-  static constexpr int kStageBytes = 2 * (kMaxCols * 128) + (kTwoSrc ? 2 : 1) * (2 * kMaxSrcRows * 128);
-  static constexpr int kStages = kTwoSrc ? 4 : 6;
-};
-constexpr int STAGES = 6;                     // upper bound over both rings
-constexpr int A_STAGES = 4;                   // TMEM A-operand ring
+constexpr int STAGES = 4;                     // SMEM ring == TMEM A ring
 constexpr int NACC = 2;                       // TMEM accumulators
-constexpr int B_TILE = kMaxCols * 128;        // 8 KB: <= 64 rows x 64 bf16
+constexpr int B_TILE = kMaxCols * 128;        // 8 KB: 64 rows x 64 bf16 (hi, then lo)
 constexpr int A_HALF = kMaxSrcRows * 128;     // 8 KB: 64 rows x 32 fp32
 constexpr int A_TILE = 2 * A_HALF;            // 16 KB
 constexpr int NUM_WARPS = 18;                 // producer, MMA, 8 drain, 8 A-operand
 constexpr int THREADS = NUM_WARPS * 32;
 constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t ACC_COL = 0;               // accumulator b at 64 b
-constexpr uint32_t A_COL = 128;               // A stage a at 128 + 64 a: hi +0..31, lo +32..63
+constexpr uint32_t ACC_COL = 0;               // accumulator b at 128 b: [0,64) hi*B+lo*Bhi, [64,128) hi*Blo
+constexpr uint32_t A_COL = 256;               // A stage s at 256 + 64 s: hi +0..31, lo +32..63
 constexpr int64_t SLICE = 16384;              // points per work item
 constexpr unsigned long long kTimeoutNs = 2000000000ull;
 
+// A stage holds B hi / lo (16 KB) + one or two FP32 source tiles (16 KB each).
+template <bool kTwoSrc> struct Ring {
+  static constexpr int kStageBytes = 2 * B_TILE + (kTwoSrc ? 2 : 1) * A_TILE;
+};
+
 struct Bars {
-  uint64_t full[STAGES];
-  uint64_t empty[STAGES];
-  uint64_t afull[A_STAGES];
-  uint64_t aempty[A_STAGES];
+  uint64_t full[STAGES];      // TMA bytes landed
+  uint64_t afull[STAGES];     // A operand of the chunk is in TMEM (8 warp arrivals)
+  uint64_t released[STAGES];  // the chunk's MMAs completed (tcgen05.commit)
   uint64_t accfull[NACC];
   uint64_t accempty[NACC];
   uint64_t done;
@@ -65,7 +67,7 @@ struct Bars {
 
 template <bool kTwoSrc>
 constexpr int smem_bytes() {
-  return Ring<kTwoSrc>::kStages * Ring<kTwoSrc>::kStageBytes + 1024 /*bars*/ + 1024 /*align*/;
+  return STAGES * Ring<kTwoSrc>::kStageBytes + 1024 /*bars*/ + 1024 /*align*/;
 }
 
 // Tensor maps of one launch: bf16 column fields with 16/32/64-row boxes, FP32 sources.
@@ -220,6 +222,28 @@ __device__ __forceinline__ void load_cols(uint32_t dst, const CUtensorMap* m16,
   }
 }
 
+// Packed FP32x2 helpers (two lanes of a 64-bit register pair).
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint32_t bf16x2_of(unsigned long long p) {
+  return pack_bf16(__uint_as_float((uint32_t)p), __uint_as_float((uint32_t)(p >> 32)));
+}
+// hi/lo split of two products held as f32x2: returns (hi bf16x2, lo bf16x2), lo = bf16(p - hi).
+__device__ __forceinline__ void split2(unsigned long long p, uint32_t& hi, uint32_t& lo) {
+  hi = bf16x2_of(p);
+  const unsigned long long g =
+      ((unsigned long long)(hi & 0xFFFF0000u) << 32) | (unsigned long long)(hi << 16);
+  lo = bf16x2_of(f2_sub(p, g));
+}
+
 // 18 warps: 5 share one SM sub-partition, whose 16K registers allow 102 per thread.
 template <bool kTwoSrc>
 __global__ void __launch_bounds__(THREADS, 1)
@@ -228,7 +252,6 @@ __global__ void __launch_bounds__(THREADS, 1)
                        const int32_t* __restrict__ map, int n_tiles, int same_src,
                        int64_t k_begin, int64_t k_end, int64_t n_items, int terms,
                        double* __restrict__ out) {
-  constexpr int STAGES = Ring<kTwoSrc>::kStages;
   constexpr int STAGE_BYTES = Ring<kTwoSrc>::kStageBytes;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
@@ -243,11 +266,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&bars->full[s], 1);
-      mbar_init(&bars->empty[s], 1 + 8);
-    }
-    for (int a = 0; a < A_STAGES; ++a) {
-      mbar_init(&bars->afull[a], 8);
-      mbar_init(&bars->aempty[a], 1);
+      mbar_init(&bars->afull[s], 8);
+      mbar_init(&bars->released[s], 1);
     }
     for (int b = 0; b < NACC; ++b) {
       mbar_init(&bars->accfull[b], 1);
@@ -280,12 +300,12 @@ __global__ void __launch_bounds__(THREADS, 1)
         const bool one_src = !kTwoSrc || (same_src && td.i0 == td.j0);
         const int64_t x_begin = k_begin + sl * SLICE;
         const int64_t x_end = min(k_end, x_begin + SLICE);
-        const uint32_t bbytes = (uint32_t)((td.nc == 64 ? 64 : td.nc) * 128);
+        const uint32_t bbytes = (uint32_t)(td.nc * 128);
         const uint32_t bytes = 2 * bbytes + (one_src ? 1u : 2u) * (uint32_t)A_TILE;
         for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
           const int s = chunk % STAGES;
           const uint32_t ph = (chunk / STAGES) & 1;
-          if (!mbar_wait(&bars->empty[s], ph ^ 1)) { ok = false; break; }
+          if (!mbar_wait(&bars->released[s], ph ^ 1)) { ok = false; break; }
           mbar_arrive_tx(&bars->full[s], bytes);
           const uint32_t st = sbase + s * STAGE_BYTES;
           const int xi = (int)x;
@@ -312,7 +332,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         const TileDesc td = tiles[item % n_tiles];
         const int64_t x_begin = k_begin + sl * SLICE;
         const int64_t x_end = min(k_end, x_begin + SLICE);
-        const uint32_t idesc = idesc_bf16(td.nc);
+        // hi x [Bhi; Blo] (rows nc..63 of the hi block are not loaded: their
+        // accumulator columns are never read), lo x Bhi
+        const uint32_t idesc_stack = idesc_bf16(terms >= 3 ? 64 + td.nc : td.nc);
+        const uint32_t idesc_hi = idesc_bf16(td.nc);
         int in_grp = 0;
         uint32_t d_tmem = 0, b = 0, accum = 0;
         for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
@@ -320,32 +343,25 @@ __global__ void __launch_bounds__(THREADS, 1)
             b = grp % NACC;
             if (!mbar_wait(&bars->accempty[b], ((grp / NACC) & 1) ^ 1)) { ok = false; break; }
             tc_fence_after();
-            d_tmem = tmem + ACC_COL + b * 64;
+            d_tmem = tmem + ACC_COL + b * 128;
             accum = 0;
           }
           const int s = chunk % STAGES;
           const uint32_t ph = (chunk / STAGES) & 1;
-          const uint32_t a = chunk % A_STAGES;
-          const uint32_t aph = (chunk / A_STAGES) & 1;
           if (!mbar_wait(&bars->full[s], ph)) { ok = false; break; }
-          if (!mbar_wait(&bars->afull[a], aph)) { ok = false; break; }
+          if (!mbar_wait(&bars->afull[s], ph)) { ok = false; break; }
           tc_fence_after();
           const uint32_t st = sbase + s * STAGE_BYTES;
-          const uint32_t a_hi = tmem + A_COL + a * 64;
+          const uint32_t a_hi = tmem + A_COL + s * 64;
           const uint32_t a_lo = a_hi + 32;
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            const uint64_t bhi = desc_sw128(st + 32 * k);
-            const uint64_t blo = desc_sw128(st + B_TILE + 32 * k);
-            mma_ts(d_tmem, a_hi + 8 * k, bhi, idesc, accum);
+            const uint64_t bdesc = desc_sw128(st + 32 * k);
+            mma_ts(d_tmem, a_hi + 8 * k, bdesc, idesc_stack, accum);
+            if (terms >= 3) mma_ts(d_tmem, a_lo + 8 * k, bdesc, idesc_hi, 1);
             accum = 1;
-            if (terms >= 3) {
-              mma_ts(d_tmem, a_hi + 8 * k, blo, idesc, 1);
-              mma_ts(d_tmem, a_lo + 8 * k, bhi, idesc, 1);
-            }
           }
-          tc_commit(&bars->empty[s]);
-          tc_commit(&bars->aempty[a]);
+          tc_commit(&bars->released[s]);
           if (++in_grp == ACC_CHUNKS || x + KCH >= x_end) {
             tc_commit(&bars->accfull[b]);
             ++grp;
@@ -386,9 +402,14 @@ __global__ void __launch_bounds__(THREADS, 1)
         for (int cc = 0; cc < 2; ++cc) {
           if (c0 + cc * 16 < td.nc) {
             uint32_t v[16];
-            tmem_ld16(taddr + ACC_COL + b * 64 + cc * 16, v);
+            tmem_ld16(taddr + ACC_COL + b * 128 + cc * 16, v);
 #pragma unroll
             for (int e = 0; e < 16; ++e) acc[cc * 16 + e] += __uint_as_float(v[e]);
+            if (terms >= 3) {
+              tmem_ld16(taddr + ACC_COL + b * 128 + 64 + cc * 16, v);
+#pragma unroll
+              for (int e = 0; e < 16; ++e) acc[cc * 16 + e] += __uint_as_float(v[e]);
+            }
           }
         }
         tc_fence_before();
@@ -428,15 +449,13 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
         const int s = chunk % STAGES;
         const uint32_t ph = (chunk / STAGES) & 1;
-        const uint32_t a = chunk % A_STAGES;
-        const uint32_t aph = (chunk / A_STAGES) & 1;
         if (!__all_sync(0xffffffffu, mbar_wait(&bars->full[s], ph))) { ok = false; break; }
-        if (!__all_sync(0xffffffffu, mbar_wait(&bars->aempty[a], aph ^ 1))) { ok = false; break; }
+        if (!__all_sync(0xffffffffu, mbar_wait(&bars->released[s], ph ^ 1))) { ok = false; break; }
         tc_fence_after();
         const uint8_t* st = smem + s * STAGE_BYTES;
         const uint8_t* row1 = st + 2 * B_TILE + half * A_HALF + pi * 128;
         const uint8_t* row2 = st + 2 * B_TILE + src2 + half * A_HALF + pj * 128;
-        const uint32_t a_hi = tmem + tlane + A_COL + a * 64 + half * 16;
+        const uint32_t a_hi = tmem + tlane + A_COL + s * 64 + half * 16;
 #pragma unroll
         for (int sub = 0; sub < 2; ++sub) {
           uint32_t hi[8], lo[8];
@@ -444,19 +463,12 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
             for (int c4 = 0; c4 < 4; ++c4) {
               const int c = sub * 4 + c4;  // logical 16-B chunk (4 floats)
-              const float4 va =
-                  *reinterpret_cast<const float4*>(row1 + ((c ^ (pi & 7)) << 4));
-              const float4 vb =
-                  *reinterpret_cast<const float4*>(row2 + ((c ^ (pj & 7)) << 4));
-              const float p0 = va.x * vb.x, p1 = va.y * vb.y;
-              const float p2 = va.z * vb.z, p3 = va.w * vb.w;
-              const uint32_t h01 = pack_bf16(p0, p1), h23 = pack_bf16(p2, p3);
-              const float g0 = __uint_as_float(h01 << 16), g1 = __uint_as_float(h01 & 0xFFFF0000u);
-              const float g2 = __uint_as_float(h23 << 16), g3 = __uint_as_float(h23 & 0xFFFF0000u);
-              hi[2 * c4] = h01;
-              hi[2 * c4 + 1] = h23;
-              lo[2 * c4] = pack_bf16(fmaf(va.x, vb.x, -g0), fmaf(va.y, vb.y, -g1));
-              lo[2 * c4 + 1] = pack_bf16(fmaf(va.z, vb.z, -g2), fmaf(va.w, vb.w, -g3));
+              const ulonglong2 va =
+                  *reinterpret_cast<const ulonglong2*>(row1 + ((c ^ (pi & 7)) << 4));
+              const ulonglong2 vb =
+                  *reinterpret_cast<const ulonglong2*>(row2 + ((c ^ (pj & 7)) << 4));
+              split2(f2_mul(va.x, vb.x), hi[2 * c4], lo[2 * c4]);
+              split2(f2_mul(va.y, vb.y), hi[2 * c4 + 1], lo[2 * c4 + 1]);
             }
           } else {
 #pragma unroll
@@ -468,10 +480,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) {
-          mbar_arrive(&bars->afull[a]);
-          mbar_arrive(&bars->empty[s]);
-        }
+        if (lane == 0) mbar_arrive(&bars->afull[s]);
       }
     }
   }

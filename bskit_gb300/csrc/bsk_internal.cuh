@@ -116,6 +116,8 @@ struct bsk_plan {
   bsk::FieldSlot slot[3];
   cufftComplex* chunk_spec = nullptr;   // [chunk][Mh] masked spectra
   int num_sms = 0;
+  float* cic_w = nullptr;               // per-axis CIC compensation factors, N+1 entries
+  int cic_nmesh = 0;                    // NmeshCIC the table was built for
   void* work = nullptr;                 // cuFFT work area shared by the plan's transforms
   size_t work_bytes = 0;
   int n_alloc() const { return (n + chunk - 1) / chunk * chunk; }  // shells rounded to batches
@@ -139,8 +141,9 @@ void launch_shell_table(const bsk_plan* p, unsigned long long* d_counts, int* d_
                         cudaStream_t st);
 // Copy the |q_c| < Ng/2 modes of an N^3 half spectrum into the Ng half grid,
 // scaled by 1/N^3.
+// axis_w: optional per-axis window factors indexed by q + N/2 (NULL = none).
 void launch_extract(const bsk_plan* p, const cufftComplex* fine, cufftComplex* coarse,
-                    cudaStream_t st);
+                    const float* axis_w, cudaStream_t st);
 // Masked spectra of shells [s0, s0+ns) into out[ns][Mh].
 void launch_filter(const bsk_plan* p, const cufftComplex* spec, int s0, int ns,
                    cufftComplex* out, cudaStream_t st);

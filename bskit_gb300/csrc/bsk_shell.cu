@@ -70,8 +70,10 @@ __global__ void shell_table_kernel(int Ng, int reduced, double kf, int n,
 
 // coarse[a][b][c] = fine[qa mod N][qb mod N][c] / N^3 for modes strictly below the coarse
 // Nyquist frequency; zero elsewhere.  When Ng == N it is a scaled copy.
+// Optional window compensation: per-axis factor table w[q + N/2], the mode's value
+// is multiplied by w[qa] w[qb] w[qc].
 __global__ void extract_kernel(int N, int Ng, float scale, const float2* __restrict__ fine,
-                               float2* __restrict__ coarse) {
+                               float2* __restrict__ coarse, const float* __restrict__ axis_w) {
   const int H = Ng / 2 + 1, HN = N / 2 + 1;
   const int64_t Mh = (int64_t)Ng * Ng * H;
   for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < Mh;
@@ -81,19 +83,21 @@ __global__ void extract_kernel(int N, int Ng, float scale, const float2* __restr
     int b = (int)(r % Ng);
     int a = (int)(r / Ng);
     float2 v = make_float2(0.f, 0.f);
+    const int qa = fft_freq(a, Ng), qb = fft_freq(b, Ng);
+    float f = scale;
+    if (axis_w) f *= axis_w[qa + N / 2] * axis_w[qb + N / 2] * axis_w[c + N / 2];
     if (Ng == N) {
       v = fine[m];
-      v.x *= scale;
-      v.y *= scale;
+      v.x *= f;
+      v.y *= f;
     } else {
-      int qa = fft_freq(a, Ng), qb = fft_freq(b, Ng);
       bool nyq = (Ng % 2 == 0) && (qa == -Ng / 2 || qb == -Ng / 2 || c == Ng / 2);
       if (!nyq) {
         int fa = qa < 0 ? qa + N : qa;
         int fb = qb < 0 ? qb + N : qb;
         v = fine[((int64_t)fa * N + fb) * HN + c];
-        v.x *= scale;
-        v.y *= scale;
+        v.x *= f;
+        v.y *= f;
       }
     }
     coarse[m] = v;
@@ -221,10 +225,11 @@ void launch_shell_table(const bsk_plan* p, unsigned long long* d_counts, int* d_
 }
 
 void launch_extract(const bsk_plan* p, const cufftComplex* fine, cufftComplex* coarse,
-                    cudaStream_t st) {
+                    const float* axis_w, cudaStream_t st) {
   float scale = (float)(1.0 / ((double)p->N * p->N * p->N));
   extract_kernel<<<grid_for(p->Mh, 256, p->num_sms * 16), 256, 0, st>>>(
-      p->N, p->Ng, scale, reinterpret_cast<const float2*>(fine), reinterpret_cast<float2*>(coarse));
+      p->N, p->Ng, scale, reinterpret_cast<const float2*>(fine), reinterpret_cast<float2*>(coarse),
+      axis_w);
   BSK_CHECK_CUDA(cudaGetLastError());
 }
 

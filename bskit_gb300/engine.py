@@ -94,12 +94,18 @@ class Plan:
         return TriangleSet(self, tri)
 
     # ------------------------------------------------------------------ compute
-    def paint(self, slot, mesh, stream=None):
-        """r2c of a real N^3 float32 CUDA tensor into field slot 0/1/2."""
+    def paint(self, slot, mesh, stream=None, cic_nmesh=None):
+        """r2c of a real N^3 float32 CUDA tensor into field slot 0/1/2.
+
+        cic_nmesh: deconvolve the CIC window of a mesh assigned on a cic_nmesh^3 grid."""
         m = self._as_mesh(mesh)
         with torch.cuda.device(self.device):
-            _lib.call("bsk_paint", self.handle, int(slot), ctypes.c_void_p(m.data_ptr()),
-                      _stream_ptr(stream))
+            if cic_nmesh:
+                _lib.call("bsk_paint_cic", self.handle, int(slot), ctypes.c_void_p(m.data_ptr()),
+                          int(cic_nmesh), _stream_ptr(stream))
+            else:
+                _lib.call("bsk_paint", self.handle, int(slot), ctypes.c_void_p(m.data_ptr()),
+                          _stream_ptr(stream))
         return m
 
     def measure_b(self, tset, slots=(0, 0, 0), precision="bf16x3", out=None, stream=None):

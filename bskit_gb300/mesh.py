@@ -11,9 +11,14 @@ import torch
 
 
 class ArrayMesh(object):
-    """A real density mesh ``array`` (N^3) in a periodic cube of side ``BoxSize``."""
+    """A real density mesh ``array`` (N^3) in a periodic cube of side ``BoxSize``.
 
-    def __init__(self, array, BoxSize):
+    ``compensate_cic``: NmeshCIC of the grid the particles were CIC-assigned on;
+    the CIC window is then deconvolved when the mesh is painted (the
+    ``CompensateCICShotnoiseNgrid`` action of scripts/measure/measure_bs_fast.py:45-57).
+    """
+
+    def __init__(self, array, BoxSize, compensate_cic=None):
         if isinstance(array, torch.Tensor):
             if array.dim() != 3 or len(set(array.shape)) != 1:
                 raise ValueError("mesh must be a cubic N^3 array")
@@ -33,6 +38,7 @@ class ArrayMesh(object):
         if box.size == 1:
             box = np.repeat(box, 3)
         self.attrs = {'Nmesh': np.array([n] * 3), 'BoxSize': box}
+        self.compensate_cic = int(compensate_cic) if compensate_cic else None
         self._cache = {}
 
     @property

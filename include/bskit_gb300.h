@@ -58,7 +58,7 @@ enum bsk_precision {
 
 /* Real-space grid the contraction runs on. */
 enum bsk_grid_mode {
-  BSK_GRID_REDUCED = 0, /* smallest FFT-friendly Ng with Ng > 3*max|q_c| (exact, see DESIGN) */
+  BSK_GRID_REDUCED = 0, /* smallest FFT-friendly Ng with Ng > 3*max|q_c| (exact: no aliasing onto the summed k=0 mode) */
   BSK_GRID_NATIVE = 1   /* Ng = N, the mesh's own grid                                   */
 };
 
@@ -78,8 +78,11 @@ int bsk_last_error(char* buf, size_t len);
  * Create a plan for an N^3 mesh in a periodic box of side L with n shells
  * [edges[2s], edges[2s+1]].  Builds the per-mode shell table on the device,
  * the exact per-shell mode counts and the cuFFT plans.
- * mem_budget: bytes of device memory the plan may hold for shell fields
- * (0 = no limit); above it the fields are streamed in shell chunks.
+ * mem_budget: bytes of device memory the plan may hold (0 = no limit).  An
+ * operation whose allocation would take the plan's footprint (BSK_INFO_FOOTPRINT)
+ * above it fails with BSK_ERR_OOM before allocating and leaves the plan usable.
+ * Like the reference, which holds every shell field of a measurement in memory,
+ * the plan keeps all n shell fields of a slot resident.
  * Replaces: FFTBispectrum.__init__ bin set-up, bskit/main.py:1485-1595, and
  *           the k-mask closures of main.py:1848-1852 / 264-268 / 314-320.
  */
@@ -116,6 +119,14 @@ int64_t bsk_triset_size(const bsk_triset* set);
  *           bskit/main.py:1608-1621.
  */
 int bsk_paint(bsk_plan* plan, int slot, const float* mesh, void* stream);
+
+/*
+ * As bsk_paint, deconvolving the CIC window of the grid the mesh was assigned
+ * on: every mode is divided by prod_c sqrt(1 - 2/3 sin^2(pi q_c / nmesh_cic)).
+ * Replaces: mesh.apply(CompensateCICShotnoiseNgrid, kind='circular',
+ *           mode='complex'), scripts/measure/measure_bs_fast.py:45-57, 218-223.
+ */
+int bsk_paint_cic(bsk_plan* plan, int slot, const float* mesh, int nmesh_cic, void* stream);
 
 /*
  * Unnormalised bispectrum of every triangle of `set`:

@@ -85,6 +85,19 @@ def spectrum(delta):
     return np.fft.rfftn(d) / d.size
 
 
+def cic_compensate(dhat, n, nmesh_cic):
+    """Divide each mode by prod_c sqrt(1 - 2/3 sin^2(w_c Nmesh / (2 NmeshCIC))), w_c = 2 pi q_c / N
+    (``CompensateCICShotnoiseNgrid``, scripts/measure/measure_bs_fast.py:45-57)."""
+    out = np.array(dhat, dtype=np.complex128, copy=True)
+    for axis, q in enumerate((freq_int(n), freq_int(n), freq_int(n, half=True))):
+        w = 2 * np.pi * q / n
+        f = (1 - 2. / 3 * np.sin(0.5 * w * n / nmesh_cic) ** 2) ** 0.5
+        shape = [1, 1, 1]
+        shape[axis] = len(q)
+        out /= f.reshape(shape)
+    return out
+
+
 def c2r(spec, n):
     """Unnormalised c2r (pmesh ``paint(mode='real')``)."""
     return np.fft.irfftn(spec, s=(n, n, n), axes=(0, 1, 2)) * float(n) ** 3

@@ -176,7 +176,11 @@ def main(ref_root):
 
     src = os.path.join(ref_root, "examples", "tests", "output_ref")
     for name in ("Lbox1000_512_kf_3kf_3lowkbins.dat", "Lbox1000_512_kf_3kf_3lowkbins_slow.dat",
-                 "Lbox1000_512_kf_3kf_3lowkbins_subbox0.dat"):
+                 "Lbox1000_512_kf_3kf_3lowkbins_subbox0.dat",
+                 # unnormalised B and its combination with the grid info (pins the combine tool)
+                 "test_grid_512_1_unnormbs_kf_3kf_3lowbins.dat",
+                 "test_grid_512_1_bs_comb_kf_3kf_3lowbins.dat",
+                 "test_grid_512_1_bs_kf_3kf_3lowbins_slow.dat"):
         shutil.copyfile(os.path.join(src, name), os.path.join(HERE, name))
     # first rows of the P(k) golden file: k_mean, P, N_modes for [0.5,1.5]kf, [1.5,2.5]kf...
     with open(os.path.join(src, "test_grid_512_1_ps_kf_0.5kf.dat")) as f:

@@ -263,3 +263,46 @@ def test_slab_ranges_sum_to_whole(cuda):
         # a different slab cut changes only the FP32 accumulation order of the tensor path
         tol = 1e-12 if prec == "fp64" else 1e-6
         assert np.abs(tot - whole).max() <= tol * np.abs(whole).max(), prec
+
+
+def test_mem_budget_refuses_before_allocating(cuda):
+    from bskit_gb300 import _lib
+    n, box, edges, tri = _small(32, 100.0, 2)
+    delta = torch.from_numpy(synthetic.lognormal_mesh(n, box, seed=21)).cuda()
+    free = Plan(n, box, edges)
+    free.paint(0, delta)
+    ref = free.measure_b(free.triangles(tri)).cpu().numpy()
+    need = free.footprint()
+    free.close()
+    tight = Plan(n, box, edges, mem_budget=need // 2)
+    tight.paint(0, delta)
+    ts = tight.triangles(tri)
+    before = tight.footprint()
+    with pytest.raises(_lib.BskError) as e:
+        tight.measure_b(ts)
+    assert e.value.code == _lib.BSK_ERR_OOM and "budget" in str(e.value)
+    assert tight.footprint() == before  # nothing was allocated
+    tight.close()
+    roomy = Plan(n, box, edges, mem_budget=need)
+    roomy.paint(0, delta)
+    # same kernels; only the order of the FP64 atomic sums may differ
+    np.testing.assert_allclose(roomy.measure_b(roomy.triangles(tri)).cpu().numpy(), ref,
+                               rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+    roomy.close()
+
+
+def test_cic_compensated_paint(cuda):
+    n, box, edges, tri = _small(32, 100.0, 2)
+    delta = synthetic.lognormal_mesh(n, box, seed=31)
+    plan = Plan(n, box, edges)
+    plan.paint(0, torch.from_numpy(delta), cic_nmesh=64)
+    ts = plan.triangles(tri)
+    b = plan.measure_b(ts, precision="fp64").cpu().numpy()
+    of = O.shell_fields(O.cic_compensate(O.spectrum(delta), n, 64), n, box, edges)
+    bo = O.triple_sums(of, of, of, tri) * box ** 6 / n ** 3
+    babs = _abs_sums(of, of, of, tri, box, n)
+    assert np.max(np.abs(b - bo) / babs) <= 2e-6
+    plain = Plan(n, box, edges)
+    plain.paint(0, torch.from_numpy(delta))
+    b0 = plain.measure_b(plain.triangles(tri), precision="fp64").cpu().numpy()
+    assert np.max(np.abs(b0 - b) / babs) > 1e-4  # the window correction is not a no-op
