@@ -55,6 +55,7 @@ SIGNATURES = [
     ("bsk_contract", _INT, [_VP, _VP, _VP, _VP, _VP, _I64, _INT, _VP, _VP]),
     ("bsk_copy_field", _INT, [_VP, _INT, _INT, _VP, _VP]),
     ("bsk_sync_check", _INT, [_VP]),
+    ("bsk_contract_noalloc", _INT, [_INT, _I64, _VP, _VP, _VP, _VP, _I64, _INT, _VP, _VP]),
 ]
 
 _lib = None

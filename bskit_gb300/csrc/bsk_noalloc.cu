@@ -1,0 +1,202 @@
+// Allocation-free tensor-core contraction: bsk_contract_noalloc.
+//
+// Some callers cannot call cudaMalloc at the moment they need a bispectrum:
+// applications whose framework reserved (nearly) all device memory in its own
+// pool at start-up, and real-time or embedded pipelines that forbid
+// cudaMalloc/cudaFree on the hot path because they synchronise the device and
+// can fail under fragmentation.  For them this file offers one entry point
+// that computes the same bf16x3 / bf16 contraction as bsk_contract but takes
+// all of its scratch -- the contraction schedule and the bf16 hi/lo split of
+// the column fields -- from one file-scope device array of fixed size
+// (kStaticScratchBytes, 64 MiB).  The caller passes the fields, the triangle
+// list and the output buffer; nothing is allocated.
+//
+// Properties callers rely on:
+//  * the array is part of this library's device image: every GPU that loads
+//    the library holds it until the process exits;
+//  * the first call on a device resolves the array's device address with
+//    cudaGetSymbolAddress (once per device, with that device current); make
+//    that first call before any stream capture;
+//  * every call shares the array and it keeps the last call's contents; each
+//    call rewrites everything it later reads (and zeroes the output), so no
+//    result depends on an earlier call -- but two calls whose work overlaps on
+//    the GPU (different streams, no ordering) race on the array;
+//  * requests that do not fit in the array are rejected with BSK_ERR_ARG.
+#include <algorithm>
+#include <map>
+
+#include "bsk_internal.cuh"
+
+namespace bsk {
+namespace {
+
+constexpr size_t kStaticScratchBytes = size_t(64) << 20;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+void* g_scratch_ptr[kMaxDevices] = {nullptr};
+
+void* scratch_address(int dev) {
+  BSK_REQUIRE(dev >= 0 && dev < kMaxDevices, BSK_ERR_UNSUPPORTED, "device ordinal above 63");
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw Error{BSK_ERR_CUDA, std::string("cudaGetSymbolAddress(static scratch): ") +
+                                    cudaGetErrorString(e)};
+    }
+    g_scratch_ptr[dev] = p;
+  }
+  return g_scratch_ptr[dev];
+}
+
+size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+// Host-side tiling of the triangle list (rows = (i, j) pairs in order of first
+// appearance, 128 per tile, column span and pair-factor spans of at most 64
+// shells) into the layouts contract_tc_kernel reads.
+struct Tables {
+  std::vector<TileDesc> tiles;
+  std::vector<int16_t> ri, rj;
+  std::vector<int32_t> map;
+};
+
+void tile_triangles(int64_t T, const int32_t* tri, int n, Tables& out) {
+  std::map<std::pair<int, int>, int> row_of;
+  std::vector<std::pair<int, int>> rows;
+  std::vector<std::vector<std::pair<int, int>>> cols;  // per row: (l, t)
+  for (int64_t t = 0; t < T; ++t) {
+    const int i = tri[3 * t], j = tri[3 * t + 1], l = tri[3 * t + 2];
+    BSK_REQUIRE(i >= 0 && j >= 0 && l >= 0 && i < n && j < n && l < n, BSK_ERR_ARG,
+                "triangle " + std::to_string(t) + " has a shell index outside [0, n_shells)");
+    auto key = std::make_pair(i, j);
+    auto it = row_of.find(key);
+    int r;
+    if (it == row_of.end()) {
+      r = (int)rows.size();
+      row_of.emplace(key, r);
+      rows.push_back(key);
+      cols.emplace_back();
+    } else {
+      r = it->second;
+    }
+    for (const auto& c : cols[r])
+      BSK_REQUIRE(c.first != l, BSK_ERR_ARG, "repeated triangle in the list");
+    cols[r].emplace_back(l, (int)t);
+  }
+  auto round16 = [](int v) { return std::max(16, (v + 15) / 16 * 16); };
+  auto round8 = [](int v) { return (v + 7) / 8 * 8; };
+  size_t r = 0;
+  while (r < rows.size()) {
+    int lmin = 1 << 30, lmax = -1, lo = 1 << 30, hi = -1;
+    size_t e = r;
+    while (e < rows.size() && e - r < (size_t)kTileRows) {
+      int nlmin = lmin, nlmax = lmax;
+      for (const auto& c : cols[e]) {
+        nlmin = std::min(nlmin, c.first);
+        nlmax = std::max(nlmax, c.first);
+      }
+      const int nlo = std::min(lo, std::min(rows[e].first, rows[e].second));
+      const int nhi = std::max(hi, std::max(rows[e].first, rows[e].second));
+      if (e > r && (round16(nlmax - nlmin + 1) > kMaxCols || nhi - nlo >= kMaxSrcRows)) break;
+      lmin = nlmin; lmax = nlmax; lo = nlo; hi = nhi;
+      ++e;
+    }
+    BSK_REQUIRE(round16(lmax - lmin + 1) <= kMaxCols && hi - lo < kMaxSrcRows,
+                BSK_ERR_UNSUPPORTED, "a pair row needs more than 64 column shells");
+    TileDesc d{};
+    d.i0 = d.j0 = lo;
+    d.ni = d.nj = round8(hi - lo + 1);
+    d.l0 = lmin;
+    d.nc = round16(lmax - lmin + 1);
+    d.nrows = (int)(e - r);
+    d.row_off = (int)out.ri.size();
+    d.map_off = (int)out.map.size();
+    out.ri.resize(out.ri.size() + kTileRows, (int16_t)-1);
+    out.rj.resize(out.rj.size() + kTileRows, (int16_t)-1);
+    out.map.resize(out.map.size() + (size_t)d.nc * kTileRows, -1);
+    for (size_t k = r; k < e; ++k) {
+      out.ri[d.row_off + (k - r)] = (int16_t)rows[k].first;
+      out.rj[d.row_off + (k - r)] = (int16_t)rows[k].second;
+      for (const auto& c : cols[k])
+        out.map[d.map_off + (size_t)(c.first - lmin) * kTileRows + (k - r)] = c.second;
+    }
+    out.tiles.push_back(d);
+    r = e;
+  }
+}
+
+}  // namespace
+}  // namespace bsk
+
+using namespace bsk;
+
+extern "C" int bsk_contract_noalloc(int n_shells, int64_t n_tri, const int32_t* tri,
+                                    const float* f1, const float* f2, const float* f3,
+                                    int64_t k_points, int precision, double* out, void* stream) {
+  cudaGetLastError();
+  try {
+    BSK_REQUIRE(n_shells >= 1 && n_shells <= 255, BSK_ERR_ARG, "need 1..255 shells");
+    BSK_REQUIRE(n_tri >= 0 && (n_tri == 0 || (tri && out)), BSK_ERR_ARG, "bad triangle list");
+    BSK_REQUIRE(f1 && f2 && f3, BSK_ERR_ARG, "NULL field pointer");
+    BSK_REQUIRE(k_points > 0 && k_points % 8 == 0, BSK_ERR_ARG,
+                "k_points must be a positive multiple of 8");
+    BSK_REQUIRE(precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16, BSK_ERR_ARG,
+                "the allocation-free contraction runs the tensor-core precisions (bf16x3, bf16)");
+    if (n_tri == 0) return BSK_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0;
+    BSK_CHECK_CUDA(cudaGetDevice(&dev));
+    int num_sms = 0;
+    BSK_CHECK_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
+
+    Tables tb;
+    tile_triangles(n_tri, tri, n_shells, tb);
+    const size_t b_tiles = align256(tb.tiles.size() * sizeof(TileDesc));
+    const size_t b_rows = align256(tb.ri.size() * sizeof(int16_t));
+    const size_t b_map = align256(tb.map.size() * sizeof(int32_t));
+    const size_t b_split = align256((size_t)n_shells * k_points * sizeof(__nv_bfloat16));
+    const size_t need = b_tiles + 2 * b_rows + b_map + 2 * b_split;
+    BSK_REQUIRE(need <= kStaticScratchBytes, BSK_ERR_ARG,
+                "request needs " + std::to_string(need) + " bytes of scratch; the static area "
+                "holds " + std::to_string(kStaticScratchBytes) + " (n_shells * k_points * 4 "
+                "bytes plus the schedule)");
+
+    unsigned char* base = (unsigned char*)scratch_address(dev);
+    DeviceSchedule s;
+    s.n_tiles = (int)tb.tiles.size();
+    s.tiles = reinterpret_cast<TileDesc*>(base);
+    s.row_i = reinterpret_cast<int16_t*>(base + b_tiles);
+    s.row_j = reinterpret_cast<int16_t*>(base + b_tiles + b_rows);
+    s.map = reinterpret_cast<int32_t*>(base + b_tiles + 2 * b_rows);
+    s.h_tiles = tb.tiles;
+    __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(base + b_tiles + 2 * b_rows + b_map);
+    __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(base + b_tiles + 2 * b_rows + b_map +
+                                                          b_split);
+    BSK_CHECK_CUDA(cudaMemcpyAsync(s.tiles, tb.tiles.data(), tb.tiles.size() * sizeof(TileDesc),
+                                   cudaMemcpyHostToDevice, st));
+    BSK_CHECK_CUDA(cudaMemcpyAsync(s.row_i, tb.ri.data(), tb.ri.size() * sizeof(int16_t),
+                                   cudaMemcpyHostToDevice, st));
+    BSK_CHECK_CUDA(cudaMemcpyAsync(s.row_j, tb.rj.data(), tb.rj.size() * sizeof(int16_t),
+                                   cudaMemcpyHostToDevice, st));
+    BSK_CHECK_CUDA(cudaMemcpyAsync(s.map, tb.map.data(), tb.map.size() * sizeof(int32_t),
+                                   cudaMemcpyHostToDevice, st));
+    // host vectors are released at return: the copies above must have read them
+    BSK_CHECK_CUDA(cudaStreamSynchronize(st));
+    launch_split(f3, hi, lo, (int64_t)n_shells * k_points, st);
+    BSK_CHECK_CUDA(cudaMemsetAsync(out, 0, (size_t)n_tri * sizeof(double), st));
+    launch_contract_tc(s, f1, f2, hi, lo, n_shells, k_points, 0, k_points,
+                       precision == BSK_PREC_BF16X3 ? 3 : 1, out, num_sms, st);
+    s.tiles = nullptr;  // the schedule lives in the static area: nothing to release
+    s.row_i = s.row_j = nullptr;
+    s.map = nullptr;
+    return BSK_OK;
+  } catch (const Error& e) {
+    set_error(e.msg);
+    return e.code;
+  } catch (const std::exception& e) {
+    set_error(e.what());
+    return BSK_ERR_ARG;
+  }
+}

@@ -195,6 +195,26 @@ int bsk_copy_field(bsk_plan* plan, int slot, int shell, float* dst, void* stream
  */
 int bsk_sync_check(void* stream);
 
+/*
+ * Allocation-free variant of bsk_contract for the tensor-core precisions
+ * (BSK_PREC_BF16X3, BSK_PREC_BF16): out[t] = sum_k f1[i_t][k] f2[j_t][k] f3[l_t][k]
+ * for n_tri host triangles (int32 [T][3] shell indices, no repeats) over
+ * device fields [n_shells][k_points].  No counterpart in the reference: it
+ * serves callers that cannot call cudaMalloc -- a process whose framework
+ * reserved the device memory up front, or a pipeline that forbids
+ * cudaMalloc/cudaFree (which synchronise and can fail) on its hot path.
+ * All scratch (the contraction schedule and the bf16 split of f3) lives in one
+ * 64 MiB static device array of the library, held by every GPU that loads the
+ * library until exit; a request needing more (about n_shells * k_points * 4
+ * bytes plus the schedule) is rejected with BSK_ERR_ARG.  The first call on a
+ * device looks up the array's address (make it before any stream capture).
+ * Calls share the array: each rewrites what it reads, but calls whose work
+ * overlaps on the GPU race.  No plan or triangle set is needed.
+ */
+int bsk_contract_noalloc(int n_shells, int64_t n_tri, const int32_t* tri, const float* f1,
+                         const float* f2, const float* f3, int64_t k_points, int precision,
+                         double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
