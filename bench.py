@@ -28,9 +28,23 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "512³ all-tri bispectra/s, bf16x3 vs FP32 at ≤1e-5 rel err; serve p50/p99 ms"
+# name -> (Nmesh, BoxSize, kmax in units of k_f, dk in units of k_f, description)
+WORKLOADS = {
+    "mesh512_all": (512, 1000.0, 128.0, 2,
+                    "512^3 all-triangle auto bispectrum: L=1000 Mpc/h, 63 shells dk=2kf from kf "
+                    "to kNyq/2, 24305 bins, lognormal float32 mesh (seed 1+rank), grid info "
+                    "cached"),
+    "mesh256_all": (256, 500.0, 64.0, 2,
+                    "256^3 all-triangle auto bispectrum: L=500 Mpc/h, 31 shells dk=2kf from kf "
+                    "to kNyq/2, 3321 bins, lognormal float32 mesh (seed 1+rank), grid info "
+                    "cached"),
+    "mesh1024_all": (1024, 2000.0, 0.3 * 512, 4,
+                     "1024^3 all-triangle auto bispectrum: L=2000 Mpc/h, 38 shells dk=4kf from "
+                     "kf to 0.3 kNyq, 5833 bins, lognormal float32 mesh (seed 1+rank), grid "
+                     "info cached"),
+}
 NMESH, BOX = 512, 1000.0
-WORKLOAD = ("512^3 all-triangle auto bispectrum: L=1000 Mpc/h, 63 shells dk=2kf from kf to "
-            "kNyq/2, 24305 bins, lognormal float32 mesh (seed 1+rank), grid info cached")
+WORKLOAD = WORKLOADS["mesh512_all"][4]
 
 
 def parse():
@@ -40,24 +54,40 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16x3")
+    ap.add_argument("--workload", default="mesh512_all", choices=sorted(WORKLOADS),
+                    help="mesh512_all is the headline; the others are smaller/larger cases "
+                         "of the same estimator (profiling, the 1024^3 grid)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the per-bin error study against the FP64 GPU contraction")
     ap.add_argument("--serve-requests", type=int, default=200,
                     help="requests of the serving leg (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=40.0, help="Poisson arrival rate, req/s")
     ap.add_argument("--serve-full", action="store_true",
                     help="serving mix with N=512 (10%%) as well; default mix is N in 64/128/256")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving leg")
+    ap.add_argument("--precision-study", action="store_true",
+                    help="run only the 512^3 cross-bispectrum precision study (equilateral, "
+                         "isosceles m=2, squeezed bins; fp32/bf16/bf16x3 vs the FP64 contraction)")
+    ap.add_argument("--precision-out", default=None,
+                    help="with --precision-study: write the per-bin errors to this JSON file")
     ap.add_argument("--no-cold", action="store_true",
                     help="profiling runs only: skip the one-off FP64 grid information and "
                          "normalise by 1 (same kernels and timings in the step)")
     return ap.parse_args()
 
 
-def workload_bins():
+def select_workload(name):
+    global NMESH, BOX, WORKLOAD
+    NMESH, BOX, _, _, WORKLOAD = WORKLOADS[name]
+
+
+def workload_bins(name="mesh512_all"):
     from bskit_gb300 import bins
-    kf = 2 * math.pi / BOX
-    kw = dict(kmin=kf, kmax=(NMESH // 4) * kf, dk=2 * kf)
+    n, box, kmax, dk, _ = WORKLOADS[name]
+    kf = 2 * math.pi / box
+    kw = dict(kmin=kf, kmax=kmax * kf, dk=dk * kf)
     return bins.generate_bin_edge_list(**kw), bins.generate_triangle_bin_list(return_indices=True,
                                                                               **kw)
 
@@ -162,7 +192,7 @@ def run_ours(args):
         if dist is not None:
             dist.barrier()
 
-    edges, tri = workload_bins()
+    edges, tri = workload_bins(args.workload)
     plan = Plan(NMESH, BOX, edges, grid="reduced", device=dev)
     ts = plan.triangles(tri)
     delta = synthetic.lognormal_mesh_torch(NMESH, BOX, seed=1 + rank, device=dev).contiguous()
@@ -249,7 +279,7 @@ def run_ours(args):
     try:
         with open(os.path.join(ROOT, "profiles", "contract_tc_traffic.json")) as f:
             tr = json.load(f)
-        traffic = tr.get("bytes_per_launch_512")
+        traffic = tr.get("bytes_per_launch", {}).get(args.workload)
     except Exception:
         pass
 
@@ -265,6 +295,35 @@ def run_ours(args):
                 "bf16x3_vs_fp32_rel_err": {"max": float(np.nanmax(rel)),
                                            "median": float(np.nanmedian(rel)),
                                            "p99": float(np.nanpercentile(rel, 99))}}
+
+    # ---- per-bin error of bf16x3 / fp32 / bf16 against the FP64 contraction of the same fields
+    precision = None
+    if not args.no_precision:
+        plan.paint(0, delta)
+        b64 = plan.measure_b(ts, precision="fp64")
+        absf = torch.stack([plan.field(0, s).abs().reshape(-1) for s in range(len(edges))])
+        babs = plan.contract(ts, absf, absf, absf, precision="fp64") * (BOX ** 6 / float(ng) ** 3)
+        del absf
+        torch.cuda.empty_cache()
+
+        live = (babs > 0) & (b64 != 0)  # bins with at least one closed triangle
+
+        def err_stats(b):
+            err = (b - b64).abs()[live]
+            nrm = err / babs[live]
+            rel = err / b64[live].abs()
+            well = b64[live].abs() >= 0.1 * babs[live]
+            return {"max_normalised": float(nrm.max()),
+                    "max_rel_well_conditioned": float(rel[well].max()) if bool(well.any()) else None,
+                    "median_rel": float(rel.median()), "p99_rel": float(rel.quantile(0.99)),
+                    "well_conditioned_bins": int(well.sum()), "bins": int(live.sum())}
+
+        precision = {"reference": "FP64 SIMT contraction of the same FP32 shell fields",
+                     "normalised": "|B - B64| / (L^6/Ng^3 sum |I_i I_j I_l|)",
+                     "well_conditioned": "|B64| >= 0.1 * L^6/Ng^3 sum |I_i I_j I_l|"}
+        for p_ in ("bf16x3", "fp32", "bf16"):
+            precision[p_] = err_stats(plan.measure_b(ts, precision=p_))
+        plan.sync_check()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -291,10 +350,11 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": prec,
         "data": "synthetic lognormal mesh (seeded), no dataset",
-        "config": {"workload": WORKLOAD, "nmesh": NMESH, "box": BOX, "n_shells": len(edges),
+        "config": {"workload": WORKLOAD, "workload_name": args.workload, "nmesh": NMESH,
+                   "box": BOX, "n_shells": len(edges),
                    "n_bins": int(len(tri)), "precision": prec, "contraction_grid": ng,
-                   "l2": "inputs larger than L2 (mesh 512 MiB, shell fields %.1f GiB)"
-                         % (len(edges) * ng ** 3 * 4 / 2 ** 30),
+                   "l2": "inputs larger than L2 (mesh %d MiB, shell fields %.1f GiB)"
+                         % (NMESH ** 3 * 4 >> 20, len(edges) * ng ** 3 * 4 / 2 ** 30),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": "bispectra/s",
                 "h2d_bytes_per_step": int(host.numel() * 4),
@@ -311,6 +371,7 @@ def run_ours(args):
         "clocks": clk,
         "cold": {"gridinfo_s": cold_gridinfo_s},
         "fp32_plain": fp32,
+        "precision_vs_fp64": precision,
     }
     if fp32:
         line["speedup_vs_fp32_plain"] = value / fp32["value"]
@@ -319,13 +380,16 @@ def run_ours(args):
         del delta, host, dmesh
         torch.cuda.empty_cache()
         line["serving"] = run_serving(args, dev)
+        if not args.no_fp32:
+            torch.cuda.empty_cache()
+            line["serving_fp32"] = run_serving(args, dev, precision="fp32")
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
 
 
-def run_serving(args, dev):
+def run_serving(args, dev, precision="bf16x3"):
     """Continuous-batching leg: seeded Poisson stream of mixed bispectrum requests.
 
     Mix: N in {64,128,256,512} with weights {.4,.3,.2,.1} (512 only with
@@ -362,7 +426,8 @@ def run_serving(args, dev):
                     squeezed_bin_index=0)
         p = pool[n]
         second = p[(i + 1) % len(p)] if cross else None
-        return serving.Request(i, p[i % len(p)], box, spec, second=second, arrival=t)
+        return serving.Request(i, p[i % len(p)], box, spec, second=second, arrival=t,
+                               precision=precision)
 
     server = serving.make_server(max_batch=4, device=dev)
     warm = []
@@ -372,7 +437,8 @@ def run_serving(args, dev):
                 spec = dict(kmin=kf, kmax=n / 4 * kf, dk=2 * kf, triangle_type=kind,
                             squeezed_bin_index=0)
                 warm.append(serving.Request(-1, pool[n][0], box, spec,
-                                            second=pool[n][1] if cross else None))
+                                            second=pool[n][1] if cross else None,
+                                            precision=precision))
     t0 = time.perf_counter()
     server.run(warm, realtime=False)
     warm_s = time.perf_counter() - t0
@@ -383,9 +449,90 @@ def run_serving(args, dev):
     stats = serving.latency_stats(reqs)
     stats.update({"rate_rps": args.serve_rate, "mix": "N %s, weights %s, 30%% cross, "
                   "all/equilateral/squeezed" % (sizes, [round(x, 3) for x in w]),
-                  "warmup_s": warm_s, "precision": "bf16x3", "max_batch": 4,
+                  "warmup_s": warm_s, "precision": precision, "max_batch": 4,
                   "resident_groups": len(server.groups)})
     return stats
+
+
+def run_precision_study(args):
+    """512^3 cross bispectrum <d1 d1 d2>, d1 lognormal (L = 1000 Mpc/h, seed 1), d2 =
+    1.5 d1 + white noise of variance 0.1 var(d1) (seed 2); bins of width 2 k_f from k_f
+    to k_Nyq/2: equilateral, isosceles m = 2 (tolerance 0.1) and squeezed with k1 in
+    [k_f, 3 k_f] (squeezed_bin_index 0).  Each precision is compared bin by bin with the
+    FP64 SIMT contraction of the same FP32 shell fields."""
+    import numpy as np
+    import torch
+
+    from bskit_gb300 import bins, synthetic
+    from bskit_gb300.engine import Plan
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    n, box = 512, 1000.0
+    kf = 2 * math.pi / box
+    kw = dict(kmin=kf, kmax=128 * kf, dk=2 * kf)
+    edges = bins.generate_bin_edge_list(**kw)
+    sets = {
+        "equilateral": bins.generate_equilateral_triangle_bin_list(return_indices=True, **kw),
+        "isosceles_m2": bins.generate_isosceles_triangle_bin_list(isos_mult=2, isos_tol=0.1,
+                                                                  return_indices=True, **kw),
+        "squeezed_k1_kf_3kf": bins.generate_squeezed_triangle_bin_list(
+            squeezed_bin_index=0, return_indices=True, **kw),
+    }
+    d1 = synthetic.lognormal_mesh_torch(n, box, seed=1, device=dev).contiguous()
+    d2 = synthetic.noisy_copy_torch(d1, seed=2).contiguous()
+    plan = Plan(n, box, edges, device=dev)
+    plan.paint(0, d1)
+    plan.paint(1, d2)
+    ng = plan.ngrid
+    scale = box ** 6 / float(ng) ** 3
+    a1 = torch.stack([plan.field(0, s_).abs().reshape(-1) for s_ in range(len(edges))])
+    a2 = torch.stack([plan.field(1, s_).abs().reshape(-1) for s_ in range(len(edges))])
+    out, per_bin = {}, {}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    for name, tri in sets.items():
+        ts = plan.triangles(tri)
+        b64 = plan.measure_b(ts, slots=(0, 0, 1), precision="fp64")
+        babs = plan.contract(ts, a1, a1, a2, precision="fp64") * scale
+        live = (babs > 0) & (b64 != 0)
+        res = {"bins": int(len(tri)), "live_bins": int(live.sum())}
+        pb = {"B_fp64": b64.cpu().tolist(), "abs_sum": babs.cpu().tolist()}
+        for prec in ("fp32", "bf16", "bf16x3"):
+            plan.measure_b(ts, slots=(0, 0, 1), precision=prec)  # warm
+            ev[0].record()
+            b = plan.measure_b(ts, slots=(0, 0, 1), precision=prec)
+            ev[1].record()
+            torch.cuda.synchronize()
+            err = (b - b64).abs()[live]
+            rel = err / b64[live].abs()
+            nrm = err / babs[live]
+            well = b64[live].abs() >= 0.1 * babs[live]
+            res[prec] = {"contraction_ms": ev[0].elapsed_time(ev[1]),
+                         "max_rel": float(rel.max()), "median_rel": float(rel.median()),
+                         "p99_rel": float(rel.quantile(0.99)),
+                         "max_rel_well_conditioned": float(rel[well].max()) if bool(well.any())
+                         else None,
+                         "well_conditioned_bins": int(well.sum()),
+                         "max_normalised": float(nrm.max())}
+            pb[prec] = b.cpu().tolist()
+        plan.sync_check()
+        ts.close()
+        out[name] = res
+        per_bin[name] = pb
+    if args.precision_out:
+        with open(args.precision_out, "w") as f:
+            json.dump({"triangles": {k: np.asarray(v).tolist() for k, v in sets.items()},
+                       "per_bin": per_bin}, f)
+    print(json.dumps({
+        "metric": "precision study: per-bin error vs the FP64 contraction of the same fields",
+        "config": {"workload": "512^3 cross bispectrum <d1 d1 d2>, L=1000 Mpc/h, d2 = 1.5 d1 + "
+                               "noise (0.1 var d1), 63 shells dk=2kf to kNyq/2",
+                   "contraction_grid": ng, "slots": "(0, 0, 1)"},
+        "reference": "FP64 SIMT contraction of the same FP32 shell fields",
+        "normalised": "|B - B64| / (L^6/Ng^3 sum |I_i I_j I_l|)",
+        "well_conditioned": "|B64| >= 0.1 * L^6/Ng^3 sum |I_i I_j I_l|",
+        "sets": out}))
+    plan.close()
 
 
 def run_reference(args):
@@ -397,7 +544,7 @@ def run_reference(args):
     from bskit_gb300 import synthetic
     from oracle.cpu_baseline import ReferenceCPU
 
-    edges, tri = workload_bins()
+    edges, tri = workload_bins(args.workload)
     delta = synthetic.lognormal_mesh(NMESH, BOX, seed=1)
     ref = ReferenceCPU(delta, BOX, edges, tri)
     try:
@@ -428,8 +575,11 @@ def run_reference(args):
 
 def main():
     args = parse()
+    select_workload(args.workload)
     if args.impl == "reference":
         run_reference(args)
+    elif args.precision_study:
+        run_precision_study(args)
     elif args.serve_only:
         import torch
         torch.cuda.set_device(0)

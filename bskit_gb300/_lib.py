@@ -28,7 +28,8 @@ PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "bf16x3": PREC_BF16X3, "bf16
 GRID_REDUCED = 0
 GRID_NATIVE = 1
 
-INFO_NMESH, INFO_NGRID, INFO_NSHELLS, INFO_QMAX, INFO_FOOTPRINT, INFO_CHUNK, INFO_DEVICE = range(7)
+INFO_NMESH, INFO_NGRID, INFO_NSHELLS, INFO_QMAX, INFO_FOOTPRINT, INFO_CHUNK, INFO_DEVICE, \
+    INFO_STREAM = range(8)
 INFO_COUNT = 8
 
 # (name, restype, argtypes) for every exported entry point
@@ -48,6 +49,8 @@ SIGNATURES = [
     ("bsk_triset_size", _I64, [_VP]),
     ("bsk_paint", _INT, [_VP, _INT, _VP, _VP]),
     ("bsk_paint_cic", _INT, [_VP, _INT, _VP, _INT, _VP]),
+    ("bsk_paint_subbox", _INT, [_VP, _INT, _VP, _INT, _INT, _INT, _INT, _VP]),
+    ("bsk_compensate_cic", _INT, [_INT, _INT, _VP, _VP, _VP]),
     ("bsk_measure_b", _INT, [_VP, _VP, _INT, _INT, _INT, _INT, _VP, _VP]),
     ("bsk_measure_b_range", _INT, [_VP, _VP, _INT, _INT, _INT, _INT, _I64, _I64, _VP, _VP]),
     ("bsk_gridinfo", _INT, [_VP, _VP, _VP, _VP, _VP]),

@@ -127,7 +127,6 @@ void bind_work(bsk_plan* p, cufftHandle h, cudaStream_t st) {
   BSK_CHECK_CUFFT(cufftSetStream(h, st));
 }
 
-// Masked shell fields of `slot` for every shell: filter kernel + batched C2R.
 // Device bytes the plan holds: shell table, filter staging, per-slot spectra,
 // fields and bf16 splits, and the shared cuFFT work area.
 int64_t footprint(const bsk_plan* p) {
@@ -137,6 +136,7 @@ int64_t footprint(const bsk_plan* p) {
     if (s.fields) fp += (int64_t)p->n_alloc() * p->K * 4;
     if (s.hi) fp += (int64_t)p->n_alloc() * p->K * 4;
   }
+  if (p->stream_C) fp += (int64_t)p->stream_C * p->K * (3 * 4 + (p->stream_tc ? 4 : 0));
   return fp + (int64_t)p->work_bytes;
 }
 
@@ -150,6 +150,18 @@ void check_budget(const bsk_plan* p, size_t bytes, const char* what) {
                                  std::to_string(p->mem_budget)};
 }
 
+void release_stream(bsk_plan* p) {
+  for (auto& b : p->stream_f) {
+    if (b.ptr) cudaFree(b.ptr);
+    b = StreamBuf{};
+  }
+  if (p->stream_split.ptr) cudaFree(p->stream_split.ptr);
+  p->stream_split = StreamBuf{};
+  p->stream_C = 0;
+  p->stream_tc = false;
+}
+
+// Masked shell fields of `slot` for every shell: filter kernel + batched C2R.
 void ensure_fields(bsk_plan* p, int s, cudaStream_t st) {
   FieldSlot& f = p->slot[s];
   BSK_REQUIRE(f.painted, BSK_ERR_STATE, "field slot " + std::to_string(s) + " was not painted");
@@ -202,9 +214,11 @@ void destroy_plan(bsk_plan* p) {
   if (p->chunk_spec) cudaFree(p->chunk_spec);
   if (p->cic_w) cudaFree(p->cic_w);
   if (p->r2c_ok) cufftDestroy(p->r2c);
+  if (p->r2c_sub_nfull) cufftDestroy(p->r2c_sub);
   if (p->c2r_ok) cufftDestroy(p->c2r);
   if (p->z2d_ok) cufftDestroy(p->z2d);
   if (p->work) cudaFree(p->work);
+  release_stream(p);
   delete p;
 }
 
@@ -244,6 +258,148 @@ void contract_dispatch(bsk_plan* p, const bsk_triset* set, const float* f1, cons
   copy_dups(set, out, st);
 }
 
+// ---------------------------------------------------------------- shell streaming
+// Triangle groups of a set for chunks of C shells: key (i/C, j/C, l/C), shells
+// rebased to their chunk, groups in lexicographic key order so that the first
+// chunk changes least often.  Built once per (set, C).
+const std::vector<StreamGroup>& stream_groups(const bsk_triset* set, int C) {
+  auto it = set->groups.find(C);
+  if (it != set->groups.end()) return it->second;
+  std::map<std::tuple<int, int, int>, std::pair<std::vector<HostTriangle>, std::vector<int>>> by;
+  for (size_t u = 0; u < set->u_tri.size(); ++u) {
+    const HostTriangle& h = set->u_tri[u];
+    auto& e = by[std::make_tuple(h.i / C, h.j / C, h.l / C)];
+    e.first.push_back(HostTriangle{h.i % C, h.j % C, h.l % C});
+    e.second.push_back(set->u_idx[u]);
+  }
+  std::vector<StreamGroup>& gs = set->groups[C];
+  gs.resize(by.size());
+  size_t g = 0;
+  for (auto& kv : by) {
+    gs[g].ca = std::get<0>(kv.first);
+    gs[g].cb = std::get<1>(kv.first);
+    gs[g].cc = std::get<2>(kv.first);
+    build_schedule(kv.second.first, C, gs[g].sched, &kv.second.second);
+    ++g;
+  }
+  return gs;
+}
+
+// FP32 fields of shells [s0, s0 + C) of `slot` into dst[C][K] (C a multiple of the
+// FFT batch); shells at or beyond n are zero.
+void chunk_fields(bsk_plan* p, int slot, int s0, int C, float* dst, cudaStream_t st) {
+  const FieldSlot& f = p->slot[slot];
+  bind_work(p, p->c2r, st);
+  for (int b = 0; b < C; b += p->chunk) {
+    const int first = s0 + b;
+    const int ns = std::max(0, std::min(p->chunk, p->n - first));
+    if (ns == 0) {
+      BSK_CHECK_CUDA(cudaMemsetAsync(dst + (size_t)b * p->K, 0,
+                                     (size_t)p->chunk * p->K * sizeof(float), st));
+      continue;
+    }
+    launch_filter(p, f.spec, first, ns, p->chunk_spec, st);
+    if (ns < p->chunk)
+      BSK_CHECK_CUDA(cudaMemsetAsync(p->chunk_spec + (size_t)ns * p->Mh, 0,
+                                     (size_t)(p->chunk - ns) * p->Mh * sizeof(cufftComplex),
+                                     st));
+    BSK_CHECK_CUFFT(cufftExecC2R(p->c2r, p->chunk_spec, dst + (size_t)b * p->K));
+  }
+}
+
+// Choose the streaming chunk: the largest multiple of the FFT batch whose buffers
+// (bytes_per_shell each) fit in what the budget leaves, at most all shells.
+int stream_chunk(const bsk_plan* p, int64_t held, size_t bytes_per_shell, const char* what) {
+  const int64_t avail = (int64_t)p->mem_budget - (footprint(p) - held);
+  int C = 0;
+  if (avail > 0) C = (int)std::min<int64_t>(avail / (int64_t)bytes_per_shell, p->n_alloc());
+  C = C / p->chunk * p->chunk;
+  if (C < p->chunk)
+    throw Error{BSK_ERR_OOM, std::string(what) + ": the budget of " +
+                                 std::to_string(p->mem_budget) + " bytes leaves room for no "
+                                 "chunk of " + std::to_string(p->chunk) + " shells"};
+  return C;
+}
+
+// Streamed B: the fields of each group's three chunks are taken from three
+// C-shell buffers, recomputed only when a buffer does not hold them.
+void measure_b_stream(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int precision,
+                      int64_t k0, int64_t k1, double* out, cudaStream_t st) {
+  const bool tc = precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16;
+  const size_t per_shell = (size_t)p->K * (3 * 4 + (tc ? 4 : 0));
+  const int64_t held = p->stream_C ? (int64_t)p->stream_C * p->K * (12 + (p->stream_tc ? 4 : 0))
+                                   : 0;
+  const int C = stream_chunk(p, held, per_shell, "shell streaming");
+  if (C != p->stream_C || (tc && !p->stream_tc)) {
+    release_stream(p);
+    for (auto& buf : p->stream_f) buf.ptr = dmalloc((size_t)C * p->K * sizeof(float));
+    if (tc) p->stream_split.ptr = dmalloc((size_t)C * p->K * 2 * sizeof(__nv_bfloat16));
+    p->stream_C = C;
+    p->stream_tc = tc;
+  }
+  const int slots[3] = {a, b, c};
+  for (int sl : slots)
+    BSK_REQUIRE(p->slot[sl].painted, BSK_ERR_STATE,
+                "field slot " + std::to_string(sl) + " was not painted");
+  auto key_of = [&](int role, int chunk) -> int64_t {
+    const int sl = slots[role];
+    return ((p->slot[sl].gen * 4 + sl) << 8) | chunk;
+  };
+  BSK_CHECK_CUDA(cudaMemsetAsync(out, 0, (size_t)set->T * sizeof(double), st));
+  const auto& groups = stream_groups(set, C);
+  for (const StreamGroup& g : groups) {
+    const int chunks[3] = {g.ca, g.cb, g.cc};
+    int64_t want[3];
+    for (int r = 0; r < 3; ++r) want[r] = key_of(r, chunks[r]);
+    // roles whose FP32 fields are read: f1, f2 always; f3 unless the split of it is current
+    const bool need3 = !tc || p->stream_split.key != want[2];
+    const float* fp[3] = {nullptr, nullptr, nullptr};
+    bool keep[3] = {false, false, false};  // buffers holding a wanted key
+    for (int r = 0; r < 3; ++r)
+      for (int q = 0; q < 3; ++q)
+        if (p->stream_f[q].key == want[r] && (r < 2 || need3)) {
+          fp[r] = (const float*)p->stream_f[q].ptr;
+          keep[q] = true;
+        }
+    for (int r = 0; r < 3; ++r) {
+      if (fp[r] || (r == 2 && !need3)) continue;
+      int q = 0;
+      while (keep[q]) ++q;  // at most three wanted keys: a free buffer exists
+      chunk_fields(p, slots[r], chunks[r] * C, C, (float*)p->stream_f[q].ptr, st);
+      p->stream_f[q].key = want[r];
+      keep[q] = true;
+      fp[r] = (const float*)p->stream_f[q].ptr;
+      for (int r2 = r + 1; r2 < 3; ++r2)
+        if (want[r2] == want[r]) fp[r2] = fp[r];
+    }
+    const __nv_bfloat16 *hi = nullptr, *lo = nullptr;
+    if (tc) {
+      __nv_bfloat16* h = (__nv_bfloat16*)p->stream_split.ptr;
+      if (p->stream_split.key != want[2]) {
+        launch_split(fp[2], h, h + (size_t)C * p->K, (int64_t)C * p->K, st);
+        p->stream_split.key = want[2];
+      }
+      hi = h;
+      lo = h + (size_t)C * p->K;
+    }
+    switch (precision) {
+      case BSK_PREC_FP64:
+        launch_contract_simt_f64(g.sched, fp[0], fp[1], fp[2], C, p->K, k0, k1, out,
+                                 p->num_sms, st);
+        break;
+      case BSK_PREC_FP32:
+        launch_contract_simt_f32(g.sched, fp[0], fp[1], fp[2], C, p->K, k0, k1, out,
+                                 p->num_sms, st);
+        break;
+      default:
+        launch_contract_tc(g.sched, fp[0], fp[1], hi, lo, C, p->K, k0, k1,
+                           precision == BSK_PREC_BF16X3 ? 3 : 1, out, p->num_sms, st);
+    }
+  }
+  copy_dups(set, out, st);
+  p->last_stream_C = C;
+}
+
 void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int precision,
                int64_t k0, int64_t k1, double* out, cudaStream_t st) {
   BSK_REQUIRE(p && set && out, BSK_ERR_ARG, "NULL argument");
@@ -252,12 +408,36 @@ void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int prec
               "slot must be 0, 1 or 2");
   BSK_REQUIRE(0 <= k0 && k0 <= k1 && k1 <= p->K, BSK_ERR_ARG, "bad point range");
   if (set->T == 0) return;
+  const bool tc = precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16;
+  BSK_REQUIRE(tc || precision == BSK_PREC_FP32 || precision == BSK_PREC_FP64, BSK_ERR_ARG,
+              "unknown precision " + std::to_string(precision));
+  if (tc) BSK_REQUIRE(k0 % 64 == 0, BSK_ERR_ARG, "tensor-core ranges must start at a multiple of 64");
+  if (p->mem_budget) {
+    // resident path: all shells of each slot (and the split of the third) stay on the device
+    const size_t field_bytes = (size_t)p->n_alloc() * p->K * sizeof(float);
+    size_t need = 0;
+    bool seen[3] = {false, false, false};
+    for (int sl : {a, b, c})
+      if (!seen[sl]) {
+        seen[sl] = true;
+        if (!p->slot[sl].fields) need += field_bytes;
+      }
+    if (tc && !p->slot[c].hi) need += field_bytes;
+    const int64_t held =
+        p->stream_C ? (int64_t)p->stream_C * p->K * (12 + (p->stream_tc ? 4 : 0)) : 0;
+    if (footprint(p) - held + (int64_t)need > (int64_t)p->mem_budget) {
+      measure_b_stream(p, set, a, b, c, precision, k0, k1, out, st);
+      launch_scale(out, set->T, std::pow(p->L, 6) / (double)p->K, st);
+      return;
+    }
+    release_stream(p);
+  }
+  p->last_stream_C = 0;
   ensure_fields(p, a, st);
   ensure_fields(p, b, st);
   ensure_fields(p, c, st);
   const __nv_bfloat16 *hi = nullptr, *lo = nullptr;
-  if (precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16) {
-    BSK_REQUIRE(k0 % 64 == 0, BSK_ERR_ARG, "tensor-core ranges must start at a multiple of 64");
+  if (tc) {
     ensure_split(p, c, st);
     hi = p->slot[c].hi;
     lo = p->slot[c].lo;
@@ -266,6 +446,93 @@ void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int prec
                     p->K, k0, k1, precision, out, st);
   const double scale = std::pow(p->L, 6) / (double)p->K;
   launch_scale(out, set->T, scale, st);
+}
+
+// Indicator (kind 0) or |k|-weighted (kind 1) FP64 fields of shells [s0, s0 + C)
+// into dst[C][K]; shells at or beyond n are zero.
+void chunk_indicator(bsk_plan* p, int kind, int s0, int C, double* dst,
+                     cufftDoubleComplex* spec, cudaStream_t st) {
+  bind_work(p, p->z2d, st);
+  for (int b = 0; b < C; b += p->chunk) {
+    const int first = s0 + b;
+    const int ns = std::max(0, std::min(p->chunk, p->n - first));
+    if (ns == 0) {
+      BSK_CHECK_CUDA(cudaMemsetAsync(dst + (size_t)b * p->K, 0,
+                                     (size_t)p->chunk * p->K * sizeof(double), st));
+      continue;
+    }
+    if (ns < p->chunk)
+      BSK_CHECK_CUDA(cudaMemsetAsync(spec + (size_t)ns * p->Mh, 0,
+                                     (size_t)(p->chunk - ns) * p->Mh * sizeof(cufftDoubleComplex),
+                                     st));
+    launch_filter_indicator(p, first, ns, kind, spec, st);
+    BSK_CHECK_CUFFT(cufftExecZ2D(p->z2d, spec, dst + (size_t)b * p->K));
+  }
+}
+
+// Streamed grid information: per triangle group, the indicator and |k| fields of
+// its (at most three) chunks sit in six C-shell FP64 buffers, recomputed only
+// when no buffer holds them.  Buffers are freed at the end.
+void gridinfo_stream(bsk_plan* p, const bsk_triset* set, double* ntri, double* kmean,
+                     cudaStream_t st) {
+  const size_t spec_bytes = (size_t)p->chunk * p->Mh * sizeof(cufftDoubleComplex);
+  const size_t fixed = spec_bytes + 3 * (size_t)set->T * sizeof(double);
+  const int64_t avail = (int64_t)p->mem_budget - footprint(p) - (int64_t)fixed;
+  const size_t per_shell = 6 * (size_t)p->K * sizeof(double);
+  int C = avail > 0 ? (int)std::min<int64_t>(avail / (int64_t)per_shell, p->n_alloc()) : 0;
+  C = C / p->chunk * p->chunk;
+  BSK_REQUIRE(C >= p->chunk, BSK_ERR_OOM,
+              "grid information: the budget of " + std::to_string(p->mem_budget) +
+                  " bytes leaves room for no chunk of " + std::to_string(p->chunk) + " shells");
+  const size_t buf_elems = (size_t)C * p->K;
+  double* pool = (double*)dmalloc_async(6 * buf_elems * sizeof(double), st);
+  cufftDoubleComplex* spec = (cufftDoubleComplex*)dmalloc_async(spec_bytes, st);
+  double* s1 = (double*)dmalloc_async(3 * (size_t)set->T * sizeof(double), st);
+  double* s2 = s1 + set->T;
+  double* s3 = s2 + set->T;
+  BSK_CHECK_CUDA(cudaMemsetAsync(ntri, 0, (size_t)set->T * sizeof(double), st));
+  BSK_CHECK_CUDA(cudaMemsetAsync(s1, 0, 3 * (size_t)set->T * sizeof(double), st));
+  int64_t held[6] = {-1, -1, -1, -1, -1, -1};
+  for (const StreamGroup& g : stream_groups(set, C)) {
+    const int chunks[3] = {g.ca, g.cb, g.cc};
+    const double* f[2][3];  // [kind][role]
+    bool keep[6] = {false, false, false, false, false, false};
+    for (int kind = 0; kind < 2; ++kind)
+      for (int r = 0; r < 3; ++r) {
+        f[kind][r] = nullptr;
+        const int64_t key = kind * 256 + chunks[r];
+        for (int q = 0; q < 6; ++q)
+          if (held[q] == key) {
+            f[kind][r] = pool + q * buf_elems;
+            keep[q] = true;
+          }
+      }
+    for (int kind = 0; kind < 2; ++kind)
+      for (int r = 0; r < 3; ++r) {
+        if (f[kind][r]) continue;
+        int q = 0;
+        while (keep[q]) ++q;  // at most six wanted keys: a free buffer exists
+        double* dst = pool + q * buf_elems;
+        chunk_indicator(p, kind, chunks[r] * C, C, dst, spec, st);
+        held[q] = kind * 256 + chunks[r];
+        keep[q] = true;
+        for (int r2 = r; r2 < 3; ++r2)
+          if (chunks[r2] == chunks[r]) f[kind][r2] = dst;
+      }
+    auto run = [&](const double* x, const double* y, const double* z, double* o) {
+      launch_contract_simt_d64(g.sched, x, y, z, C, p->K, 0, p->K, o, p->num_sms, st);
+    };
+    run(f[0][0], f[0][1], f[0][2], ntri);
+    run(f[1][0], f[0][1], f[0][2], s1);
+    run(f[0][0], f[1][1], f[0][2], s2);
+    run(f[0][0], f[0][1], f[1][2], s3);
+  }
+  for (double* o : {ntri, s1, s2, s3}) copy_dups(set, o, st);
+  launch_gridinfo_finish(set->T, 1.0 / (double)p->K, ntri, s1, s2, s3, kmean, st);
+  BSK_CHECK_CUDA(cudaFreeAsync(s1, st));
+  BSK_CHECK_CUDA(cudaFreeAsync(spec, st));
+  BSK_CHECK_CUDA(cudaFreeAsync(pool, st));
+  p->last_stream_C = C;
 }
 
 }  // namespace
@@ -370,7 +637,7 @@ int bsk_plan_query(const bsk_plan* p, int64_t* info) {
     info[BSK_INFO_FOOTPRINT] = fp;
     info[BSK_INFO_CHUNK] = p->chunk;
     info[BSK_INFO_DEVICE] = p->device;
-    info[7] = 0;
+    info[BSK_INFO_STREAM] = p->last_stream_C;
   });
 }
 
@@ -392,10 +659,7 @@ int bsk_triset_create(bsk_plan* p, int64_t n_tri, const int32_t* tri, bsk_triset
     s->plan = p;
     s->T = n_tri;
     std::map<std::tuple<int, int, int>, int> first;
-    std::vector<HostTriangle> uniq;
     std::vector<int2> dups;
-    std::vector<HostTriangle> sched_tri;
-    std::vector<int> sched_t;
     for (int64_t t = 0; t < n_tri; ++t) {
       HostTriangle h{tri[3 * t], tri[3 * t + 1], tri[3 * t + 2]};
       BSK_REQUIRE(h.i >= 0 && h.j >= 0 && h.l >= 0 && h.i < p->n && h.j < p->n && h.l < p->n,
@@ -412,31 +676,16 @@ int bsk_triset_create(bsk_plan* p, int64_t n_tri, const int32_t* tri, bsk_triset
       }
     }
     // schedule over unique triangles; map entries carry the first index
-    std::vector<HostTriangle> u_tri;
-    std::vector<int> u_idx;
     {
-      // keep original order of first occurrences
       std::vector<char> is_first(n_tri, 0);
       for (auto& kv : first) is_first[kv.second] = 1;
       for (int64_t t = 0; t < n_tri; ++t)
         if (is_first[t]) {
-          u_tri.push_back(s->tri[t]);
-          u_idx.push_back((int)t);
+          s->u_tri.push_back(s->tri[t]);
+          s->u_idx.push_back((int)t);
         }
     }
-    build_schedule(u_tri, p->n, s->sched);
-    // remap map entries (indices into u_tri) to original triangle indices
-    if (!u_tri.empty() && s->sched.n_tiles > 0) {
-      size_t total = 0;
-      for (auto& d : s->sched.h_tiles) total += (size_t)d.nc * kTileRows;
-      std::vector<int32_t> m(total);
-      BSK_CHECK_CUDA(cudaMemcpy(m.data(), s->sched.map, total * sizeof(int32_t),
-                                cudaMemcpyDeviceToHost));
-      for (auto& v : m)
-        if (v >= 0) v = u_idx[v];
-      BSK_CHECK_CUDA(cudaMemcpy(s->sched.map, m.data(), total * sizeof(int32_t),
-                                cudaMemcpyHostToDevice));
-    }
+    build_schedule(s->u_tri, p->n, s->sched, &s->u_idx);
     if (!dups.empty()) {
       s->n_dups = (int)dups.size();
       s->dups = (int2*)dmalloc(dups.size() * sizeof(int2));
@@ -452,6 +701,8 @@ int bsk_triset_destroy(bsk_triset* set) {
     if (!set) return;
     DeviceGuard g(set->plan->device);
     set->sched.release();
+    for (auto& kv : set->groups)
+      for (auto& g : kv.second) g.sched.release();
     if (set->dups) cudaFree(set->dups);
     delete set;
   });
@@ -477,7 +728,27 @@ void ensure_cic_table(bsk_plan* p, int nmesh_cic) {
   p->cic_nmesh = nmesh_cic;
 }
 
-void paint(bsk_plan* p, int slot, const float* mesh, int nmesh_cic, cudaStream_t st) {
+// R2C of an N^3 block of a larger nfull^3 mesh, read in place (strided input).
+void make_r2c_sub(bsk_plan* p, int nfull) {
+  if (p->r2c_sub_nfull == nfull) return;
+  if (p->r2c_sub_nfull) cufftDestroy(p->r2c_sub);
+  p->r2c_sub_nfull = 0;
+  long long n[3] = {p->N, p->N, p->N};
+  long long inembed[3] = {nfull, nfull, nfull};
+  long long onembed[3] = {p->N, p->N, p->N / 2 + 1};
+  const long long idist = (long long)nfull * nfull * nfull;
+  const long long odist = (long long)p->N * p->N * (p->N / 2 + 1);
+  BSK_CHECK_CUFFT(cufftCreate(&p->r2c_sub));
+  p->r2c_sub_nfull = nfull;
+  BSK_CHECK_CUFFT(cufftSetAutoAllocation(p->r2c_sub, 0));
+  size_t ws = 0;
+  BSK_CHECK_CUFFT(cufftMakePlanMany64(p->r2c_sub, 3, n, inembed, 1, idist, onembed, 1, odist,
+                                      CUFFT_R2C, 1, &ws));
+  grow_work(p, ws);
+}
+
+void paint(bsk_plan* p, int slot, const float* mesh, int nmesh_cic, cudaStream_t st,
+           int nfull = 0) {
   BSK_REQUIRE(p && mesh, BSK_ERR_ARG, "NULL argument");
   BSK_REQUIRE(slot >= 0 && slot < 3, BSK_ERR_ARG, "slot must be 0, 1 or 2");
   FieldSlot& f = p->slot[slot];
@@ -486,14 +757,17 @@ void paint(bsk_plan* p, int slot, const float* mesh, int nmesh_cic, cudaStream_t
     ensure_cic_table(p, nmesh_cic);
     axis_w = p->cic_w;
   }
+  if (nfull) make_r2c_sub(p, nfull);
+  cufftHandle h = nfull ? p->r2c_sub : p->r2c;
   size_t fine_elems = (size_t)p->N * p->N * (p->N / 2 + 1);
   cufftComplex* fine = (cufftComplex*)dmalloc_async(fine_elems * sizeof(cufftComplex), st);
-  bind_work(p, p->r2c, st);
-  BSK_CHECK_CUFFT(cufftExecR2C(p->r2c, const_cast<float*>(mesh), fine));
+  bind_work(p, h, st);
+  BSK_CHECK_CUFFT(cufftExecR2C(h, const_cast<float*>(mesh), fine));
   if (!f.spec) f.spec = (cufftComplex*)dmalloc((size_t)p->Mh * sizeof(cufftComplex));
   launch_extract(p, fine, f.spec, axis_w, st);
   BSK_CHECK_CUDA(cudaFreeAsync(fine, st));
   f.painted = true;
+  ++f.gen;
   f.fields_ok = false;
   f.split_ok = false;
 }
@@ -514,6 +788,72 @@ int bsk_paint_cic(bsk_plan* p, int slot, const float* mesh, int nmesh_cic, void*
     BSK_REQUIRE(nmesh_cic > 0, BSK_ERR_ARG, "NmeshCIC must be positive");
     DeviceGuard g(p->device);
     paint(p, slot, mesh, nmesh_cic, (cudaStream_t)stream);
+  });
+}
+
+int bsk_paint_subbox(bsk_plan* p, int slot, const float* mesh, int nmesh_full, int a, int b,
+                     int c, void* stream) {
+  return guarded([&] {
+    BSK_REQUIRE(p && mesh, BSK_ERR_ARG, "NULL argument");
+    BSK_REQUIRE(nmesh_full >= p->N && nmesh_full % p->N == 0, BSK_ERR_ARG,
+                "the full mesh side must be a multiple of the plan's Nmesh");
+    const int nsub = nmesh_full / p->N;
+    BSK_REQUIRE(a >= 0 && b >= 0 && c >= 0 && a < nsub && b < nsub && c < nsub, BSK_ERR_ARG,
+                "sub-box index outside [0, nmesh_full / Nmesh)");
+    DeviceGuard g(p->device);
+    const int64_t n = p->N, nf = nmesh_full;
+    const float* origin = mesh + ((a * n) * nf + b * n) * nf + c * n;
+    paint(p, slot, origin, 0, (cudaStream_t)stream, nmesh_full);
+  });
+}
+
+int bsk_compensate_cic(int nmesh, int nmesh_cic, const float* mesh, float* out, void* stream) {
+  return guarded([&] {
+    BSK_REQUIRE(mesh && out, BSK_ERR_ARG, "NULL argument");
+    BSK_REQUIRE(nmesh >= 2 && nmesh % 2 == 0 && nmesh <= 4096, BSK_ERR_ARG,
+                "Nmesh must be even, 2..4096");
+    BSK_REQUIRE(nmesh_cic > 0, BSK_ERR_ARG, "NmeshCIC must be positive");
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    BSK_CHECK_CUDA(cudaGetDevice(&dev));
+    BSK_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    std::vector<float> w(nmesh + 1);
+    for (int i = 0; i <= nmesh; ++i) {
+      const double sn = std::sin(3.14159265358979323846 * (i - nmesh / 2) / nmesh_cic);
+      w[i] = (float)(1.0 / std::sqrt(1.0 - 2.0 / 3.0 * sn * sn));
+    }
+    const size_t mh = (size_t)nmesh * nmesh * (nmesh / 2 + 1);
+    cufftHandle fwd = 0, inv = 0;
+    bool fwd_ok = false, inv_ok = false;
+    float* dw = nullptr;
+    cufftComplex* spec = nullptr;
+    try {
+      BSK_CHECK_CUFFT(cufftPlan3d(&fwd, nmesh, nmesh, nmesh, CUFFT_R2C));
+      fwd_ok = true;
+      BSK_CHECK_CUFFT(cufftPlan3d(&inv, nmesh, nmesh, nmesh, CUFFT_C2R));
+      inv_ok = true;
+      BSK_CHECK_CUFFT(cufftSetStream(fwd, st));
+      BSK_CHECK_CUFFT(cufftSetStream(inv, st));
+      dw = (float*)dmalloc_async(w.size() * sizeof(float), st);
+      spec = (cufftComplex*)dmalloc_async(mh * sizeof(cufftComplex), st);
+      BSK_CHECK_CUDA(cudaMemcpyAsync(dw, w.data(), w.size() * sizeof(float),
+                                     cudaMemcpyHostToDevice, st));
+      BSK_CHECK_CUFFT(cufftExecR2C(fwd, const_cast<float*>(mesh), spec));
+      launch_window(nmesh, (float)(1.0 / ((double)nmesh * nmesh * nmesh)), spec, dw, sms, st);
+      BSK_CHECK_CUFFT(cufftExecC2R(inv, spec, out));
+      // the host table must outlive its copy; the plans are destroyed after the work
+      BSK_CHECK_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+      if (spec) cudaFreeAsync(spec, st);
+      if (dw) cudaFreeAsync(dw, st);
+      if (fwd_ok) cufftDestroy(fwd);
+      if (inv_ok) cufftDestroy(inv);
+      throw;
+    }
+    BSK_CHECK_CUDA(cudaFreeAsync(spec, st));
+    BSK_CHECK_CUDA(cudaFreeAsync(dw, st));
+    cufftDestroy(fwd);
+    cufftDestroy(inv);
   });
 }
 
@@ -568,8 +908,13 @@ int bsk_gridinfo(bsk_plan* p, const bsk_triset* set, double* ntri, double* kmean
     make_z2d(p);
     bind_work(p, p->z2d, st);
     const size_t fbytes = (size_t)p->n_alloc() * p->K * sizeof(double);
-    check_budget(p, 2 * fbytes + (size_t)p->chunk * p->Mh * sizeof(cufftDoubleComplex),
-                 "the FP64 counting fields of the grid information");
+    const size_t spec_bytes = (size_t)p->chunk * p->Mh * sizeof(cufftDoubleComplex);
+    if (p->mem_budget && footprint(p) + (int64_t)(2 * fbytes + spec_bytes + 24 * set->T) >
+                             (int64_t)p->mem_budget) {
+      gridinfo_stream(p, set, ntri, kmean, st);
+      return;
+    }
+    p->last_stream_C = 0;
     double* nf = (double*)dmalloc_async(fbytes, st);
     double* kf = (double*)dmalloc_async(fbytes, st);
     cufftDoubleComplex* spec = (cufftDoubleComplex*)dmalloc_async(

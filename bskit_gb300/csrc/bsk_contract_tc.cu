@@ -5,15 +5,16 @@
 // One persistent CTA per SM walks work items (tile of 128 pair rows x nc <= 64
 // columns, K slice of SLICE points), slice-major so that the CTAs running at
 // the same time share field data in L2.  Per 64-point chunk:
-//   * warp 0 (one lane) TMA-loads into a 4-stage SMEM ring the bf16 hi and lo
-//     tiles of the column fields as one 128-row operand (rows 0..63 hi, 64..127
-//     lo; SWIZZLE_128B, K-major) and the FP32 tile(s) of the pair-factor shells
-//     (one 64-shell tile when one range covers both factors of every row, as for
-//     auto spectra);
+//   * warp 0 (one lane) TMA-loads into an SMEM ring (6 stages with one source
+//     tile, 4 with two) the bf16 hi and lo tiles of the column fields as one
+//     128-row operand (rows 0..63 hi, 64..127 lo; SWIZZLE_128B, K-major) and
+//     the FP32 tile(s) of the pair-factor shells (one tile when one range covers
+//     both factors of every row, as for auto spectra), each with only as many
+//     shell rows (16/32/48/64) as the tile uses;
 //   * warps 10..17 (2 per TMEM lane quadrant, one 32-point half each) read the
 //     row's F1_i, F2_j from SMEM, form P = F1_i*F2_j with packed f32x2
 //     arithmetic, split P = hi + lo (bf16 round-to-nearest) and store them with
-//     tcgen05.st into the TMEM A-operand ring (lane = GEMM row);
+//     tcgen05.st into the 4-stage TMEM A-operand ring (lane = GEMM row);
 //   * warp 1 (one lane) issues, per 16-point K step, tcgen05.mma kind::f16 with
 //     A from TMEM and B from SMEM: hi x [Bhi; Blo] (N = 64 + nc: one MMA yields
 //     both hi*Bhi and hi*Blo) and, for bf16x3, lo x Bhi (N = nc).  The tensor
@@ -24,8 +25,10 @@
 //     add it into per-thread FP32 registers (round-to-nearest), and at the end
 //     of the slice add the entries that are triangle bins into the FP64 output
 //     (atomics).
-// One mbarrier per stage carries the MMAs' completion back to both the TMA
-// producer (SMEM stage free) and the A-operand warps (TMEM stage free).  Every
+// The MMAs' completion is committed to two mbarriers per chunk: one frees the
+// SMEM stage for the TMA producer, one frees the TMEM A stage for the A-operand
+// warps; the SMEM ring runs deeper than the TMEM ring so that more loads are in
+// flight than A stages exist.  Every
 // wait is bounded (globaltimer); on expiry the kernel records an error flag,
 // stops issuing work, drains its own MMAs and frees TMEM.
 #include <cuda.h>
@@ -37,7 +40,7 @@ namespace tc {
 
 constexpr int KCH = 64;                       // points per chunk
 constexpr int ACC_CHUNKS = 2;                 // chunks summed inside one TMEM accumulator
-constexpr int STAGES = 4;                     // SMEM ring == TMEM A ring
+constexpr int ASTAGES = 4;                    // TMEM A-operand ring
 constexpr int NACC = 2;                       // TMEM accumulators
 constexpr int B_TILE = kMaxCols * 128;        // 8 KB: 64 rows x 64 bf16 (hi, then lo)
 constexpr int A_HALF = kMaxSrcRows * 128;     // 8 KB: 64 rows x 32 fp32
@@ -50,15 +53,18 @@ constexpr uint32_t A_COL = 256;               // A stage s at 256 + 64 s: hi +0.
 constexpr int64_t SLICE = 16384;              // points per work item
 constexpr unsigned long long kTimeoutNs = 2000000000ull;
 
-// A stage holds B hi / lo (16 KB) + one or two FP32 source tiles (16 KB each).
+// An SMEM stage holds B hi / lo (16 KB) + one or two FP32 source tiles (16 KB each).
 template <bool kTwoSrc> struct Ring {
   static constexpr int kStageBytes = 2 * B_TILE + (kTwoSrc ? 2 : 1) * A_TILE;
+  static constexpr int kStages = kTwoSrc ? 4 : 6;
 };
+constexpr int MAX_SSTAGES = 6;
 
 struct Bars {
-  uint64_t full[STAGES];      // TMA bytes landed
-  uint64_t afull[STAGES];     // A operand of the chunk is in TMEM (8 warp arrivals)
-  uint64_t released[STAGES];  // the chunk's MMAs completed (tcgen05.commit)
+  uint64_t full[MAX_SSTAGES];      // TMA bytes landed
+  uint64_t released[MAX_SSTAGES];  // the MMAs reading the SMEM stage completed (tcgen05.commit)
+  uint64_t afull[ASTAGES];         // A operand of the chunk is in TMEM (8 warp arrivals)
+  uint64_t aempty[ASTAGES];        // the MMAs reading the TMEM A stage completed
   uint64_t accfull[NACC];
   uint64_t accempty[NACC];
   uint64_t done;
@@ -67,12 +73,12 @@ struct Bars {
 
 template <bool kTwoSrc>
 constexpr int smem_bytes() {
-  return STAGES * Ring<kTwoSrc>::kStageBytes + 1024 /*bars*/ + 1024 /*align*/;
+  return Ring<kTwoSrc>::kStages * Ring<kTwoSrc>::kStageBytes + 1024 /*bars*/ + 1024 /*align*/;
 }
 
-// Tensor maps of one launch: bf16 column fields with 16/32/64-row boxes, FP32 sources.
+// Tensor maps of one launch: bf16 column fields and FP32 sources, 16/32/64-row boxes.
 struct Maps {
-  CUtensorMap hi16, hi32, hi64, lo16, lo32, lo64, f1, f2;
+  CUtensorMap hi16, hi32, hi64, lo16, lo32, lo64, f1_16, f1_32, f1_64, f2_16, f2_32, f2_64;
 };
 
 __device__ int g_tc_error;  // 0 ok, 1 a bounded wait expired
@@ -209,14 +215,19 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   return *reinterpret_cast<uint32_t*>(&h);
 }
 
-__device__ __forceinline__ void load_cols(uint32_t dst, const CUtensorMap* m16,
+// Rows a load of `n` shell rows covers: 16, 32, 48 (32 + 16) or 64.
+__host__ __device__ __forceinline__ int box_rows(int n) {
+  return n <= 16 ? 16 : n <= 32 ? 32 : n <= 48 ? 48 : 64;
+}
+// Load rows [y, y + box_rows(n)) of 128-B rows at x into dst (SWIZZLE_128B layout).
+__device__ __forceinline__ void load_rows(uint32_t dst, const CUtensorMap* m16,
                                           const CUtensorMap* m32, const CUtensorMap* m64,
-                                          uint64_t* bar, int x, int y, int nc) {
-  if (nc == 64) {
+                                          uint64_t* bar, int x, int y, int n) {
+  if (n > 48) {
     tma_load_2d(dst, m64, bar, x, y);
-  } else if (nc >= 32) {
+  } else if (n > 16) {
     tma_load_2d(dst, m32, bar, x, y);
-    if (nc == 48) tma_load_2d(dst + 32 * 128, m16, bar, x, y + 32);
+    if (n > 32) tma_load_2d(dst + 32 * 128, m16, bar, x, y + 32);
   } else {
     tma_load_2d(dst, m16, bar, x, y);
   }
@@ -253,21 +264,25 @@ __global__ void __launch_bounds__(THREADS, 1)
                        int64_t k_begin, int64_t k_end, int64_t n_items, int terms,
                        double* __restrict__ out) {
   constexpr int STAGE_BYTES = Ring<kTwoSrc>::kStageBytes;
+  constexpr int SST = Ring<kTwoSrc>::kStages;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
   uint8_t* smem = smem_raw + pad;
-  Bars* bars = reinterpret_cast<Bars*>(smem + STAGES * STAGE_BYTES);
+  Bars* bars = reinterpret_cast<Bars*>(smem + SST * STAGE_BYTES);
   const uint32_t sbase = raw + pad;
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
+    for (int s = 0; s < SST; ++s) {
       mbar_init(&bars->full[s], 1);
-      mbar_init(&bars->afull[s], 8);
       mbar_init(&bars->released[s], 1);
+    }
+    for (int a = 0; a < ASTAGES; ++a) {
+      mbar_init(&bars->afull[a], 8);
+      mbar_init(&bars->aempty[a], 1);
     }
     for (int b = 0; b < NACC; ++b) {
       mbar_init(&bars->accfull[b], 1);
@@ -300,24 +315,26 @@ __global__ void __launch_bounds__(THREADS, 1)
         const bool one_src = !kTwoSrc || (same_src && td.i0 == td.j0);
         const int64_t x_begin = k_begin + sl * SLICE;
         const int64_t x_end = min(k_end, x_begin + SLICE);
-        const uint32_t bbytes = (uint32_t)(td.nc * 128);
-        const uint32_t bytes = 2 * bbytes + (one_src ? 1u : 2u) * (uint32_t)A_TILE;
+        // bytes per chunk: the column rows of hi and lo, both halves of each source tile
+        const uint32_t bytes =
+            (uint32_t)(2 * box_rows(td.nc) * 128 +
+                       2 * 128 * (box_rows(td.ni) + (one_src ? 0 : box_rows(td.nj))));
         for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
-          const int s = chunk % STAGES;
-          const uint32_t ph = (chunk / STAGES) & 1;
+          const int s = chunk % SST;
+          const uint32_t ph = (chunk / SST) & 1;
           if (!mbar_wait(&bars->released[s], ph ^ 1)) { ok = false; break; }
           mbar_arrive_tx(&bars->full[s], bytes);
           const uint32_t st = sbase + s * STAGE_BYTES;
           const int xi = (int)x;
-          load_cols(st, &maps.hi16, &maps.hi32, &maps.hi64, &bars->full[s], xi, td.l0, td.nc);
-          load_cols(st + B_TILE, &maps.lo16, &maps.lo32, &maps.lo64, &bars->full[s], xi, td.l0,
+          load_rows(st, &maps.hi16, &maps.hi32, &maps.hi64, &bars->full[s], xi, td.l0, td.nc);
+          load_rows(st + B_TILE, &maps.lo16, &maps.lo32, &maps.lo64, &bars->full[s], xi, td.l0,
                     td.nc);
           for (int h = 0; h < 2; ++h) {
-            tma_load_2d(st + 2 * B_TILE + h * A_HALF, &maps.f1, &bars->full[s], xi + 32 * h,
-                        td.i0);
+            load_rows(st + 2 * B_TILE + h * A_HALF, &maps.f1_16, &maps.f1_32, &maps.f1_64,
+                      &bars->full[s], xi + 32 * h, td.i0, td.ni);
             if (!one_src)
-              tma_load_2d(st + 2 * B_TILE + A_TILE + h * A_HALF, &maps.f2, &bars->full[s],
-                          xi + 32 * h, td.j0);
+              load_rows(st + 2 * B_TILE + A_TILE + h * A_HALF, &maps.f2_16, &maps.f2_32,
+                        &maps.f2_64, &bars->full[s], xi + 32 * h, td.j0, td.nj);
           }
         }
       }
@@ -346,13 +363,15 @@ __global__ void __launch_bounds__(THREADS, 1)
             d_tmem = tmem + ACC_COL + b * 128;
             accum = 0;
           }
-          const int s = chunk % STAGES;
-          const uint32_t ph = (chunk / STAGES) & 1;
+          const int s = chunk % SST;
+          const uint32_t ph = (chunk / SST) & 1;
+          const int a = chunk % ASTAGES;
+          const uint32_t pa = (chunk / ASTAGES) & 1;
           if (!mbar_wait(&bars->full[s], ph)) { ok = false; break; }
-          if (!mbar_wait(&bars->afull[s], ph)) { ok = false; break; }
+          if (!mbar_wait(&bars->afull[a], pa)) { ok = false; break; }
           tc_fence_after();
           const uint32_t st = sbase + s * STAGE_BYTES;
-          const uint32_t a_hi = tmem + A_COL + s * 64;
+          const uint32_t a_hi = tmem + A_COL + a * 64;
           const uint32_t a_lo = a_hi + 32;
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
@@ -362,6 +381,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             accum = 1;
           }
           tc_commit(&bars->released[s]);
+          tc_commit(&bars->aempty[a]);
           if (++in_grp == ACC_CHUNKS || x + KCH >= x_end) {
             tc_commit(&bars->accfull[b]);
             ++grp;
@@ -447,15 +467,17 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int pj = valid ? rj - td.j0 : 0;
       const int src2 = one_src ? 0 : A_TILE;
       for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
-        const int s = chunk % STAGES;
-        const uint32_t ph = (chunk / STAGES) & 1;
+        const int s = chunk % SST;
+        const uint32_t ph = (chunk / SST) & 1;
+        const int a = chunk % ASTAGES;
+        const uint32_t pa = (chunk / ASTAGES) & 1;
         if (!__all_sync(0xffffffffu, mbar_wait(&bars->full[s], ph))) { ok = false; break; }
-        if (!__all_sync(0xffffffffu, mbar_wait(&bars->released[s], ph ^ 1))) { ok = false; break; }
+        if (!__all_sync(0xffffffffu, mbar_wait(&bars->aempty[a], pa ^ 1))) { ok = false; break; }
         tc_fence_after();
         const uint8_t* st = smem + s * STAGE_BYTES;
         const uint8_t* row1 = st + 2 * B_TILE + half * A_HALF + pi * 128;
         const uint8_t* row2 = st + 2 * B_TILE + src2 + half * A_HALF + pj * 128;
-        const uint32_t a_hi = tmem + tlane + A_COL + s * 64 + half * 16;
+        const uint32_t a_hi = tmem + tlane + A_COL + a * 64 + half * 16;
 #pragma unroll
         for (int sub = 0; sub < 2; ++sub) {
           uint32_t hi[8], lo[8];
@@ -480,7 +502,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&bars->afull[s]);
+        if (lane == 0) mbar_arrive(&bars->afull[a]);
       }
     }
   }
@@ -547,16 +569,25 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
   tc::make_map(&m.lo16, BF, 2, f3_lo, K, n_shells, 64, 16);
   tc::make_map(&m.lo32, BF, 2, f3_lo, K, n_shells, 64, 32);
   tc::make_map(&m.lo64, BF, 2, f3_lo, K, n_shells, 64, 64);
-  tc::make_map(&m.f1, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, f1, K, n_shells, 32, 64);
-  tc::make_map(&m.f2, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, f2, K, n_shells, 32, 64);
+  const auto F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  tc::make_map(&m.f1_16, F32, 4, f1, K, n_shells, 32, 16);
+  tc::make_map(&m.f1_32, F32, 4, f1, K, n_shells, 32, 32);
+  tc::make_map(&m.f1_64, F32, 4, f1, K, n_shells, 32, 64);
+  tc::make_map(&m.f2_16, F32, 4, f2, K, n_shells, 32, 16);
+  tc::make_map(&m.f2_32, F32, 4, f2, K, n_shells, 32, 32);
+  tc::make_map(&m.f2_64, F32, 4, f2, K, n_shells, 32, 64);
   bool two_src = f1 != f2;
   for (const TileDesc& d : s.h_tiles) two_src = two_src || d.i0 != d.j0;
-  static bool attr_set[2] = {false, false};
+  constexpr int kMaxDev = 64;
+  static bool attr_set[kMaxDev][2] = {};
+  int dev = 0;
+  BSK_CHECK_CUDA(cudaGetDevice(&dev));
+  BSK_REQUIRE(dev < kMaxDev, BSK_ERR_UNSUPPORTED, "device ordinal above 63");
   auto kern = two_src ? tc::contract_tc_kernel<true> : tc::contract_tc_kernel<false>;
   const int smem = two_src ? tc::smem_bytes<true>() : tc::smem_bytes<false>();
-  if (!attr_set[two_src]) {
+  if (!attr_set[dev][two_src]) {
     BSK_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    attr_set[two_src] = true;
+    attr_set[dev][two_src] = true;
   }
   const int64_t n_slices = (k_end - k_begin + tc::SLICE - 1) / tc::SLICE;
   const int64_t n_items = n_slices * s.n_tiles;

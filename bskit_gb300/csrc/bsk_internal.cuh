@@ -5,6 +5,7 @@
 #include <cufft.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -76,8 +77,24 @@ struct HostTriangle {
 };
 
 // Build the tile schedule for a triangle list (host).  `n_shells` bounds the
-// indices.  Rows with identical (i, j) share one pair product.
-void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSchedule& out);
+// indices.  Rows with identical (i, j) share one pair product.  Map entries are
+// positions in `tri`, or map_index[position] when map_index is given.
+void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSchedule& out,
+                    const std::vector<int>* map_index = nullptr);
+
+// Shell streaming: the triangles whose shells fall in chunks (ca, cb, cc) of C
+// shells each, scheduled with shell indices relative to their chunk.
+struct StreamGroup {
+  int ca = 0, cb = 0, cc = 0;
+  DeviceSchedule sched;
+};
+
+// Device buffers of C shells each that hold streamed shell fields, with the
+// identity of what each holds (-1 = nothing).
+struct StreamBuf {
+  void* ptr = nullptr;
+  int64_t key = -1;
+};
 
 // ---------------------------------------------------------------- plan
 struct FieldSlot {
@@ -88,6 +105,7 @@ struct FieldSlot {
   __nv_bfloat16* lo = nullptr;
   bool fields_ok = false;
   bool split_ok = false;
+  int64_t gen = 0;                // bumped by every paint (keys of streamed fields)
 };
 
 }  // namespace bsk
@@ -109,6 +127,8 @@ struct bsk_plan {
   double* d_edges = nullptr;  // device [2n]
   cufftHandle r2c = 0;        // N^3 R2C
   bool r2c_ok = false;
+  cufftHandle r2c_sub = 0;    // N^3 R2C of a block of a larger mesh (strided input)
+  int r2c_sub_nfull = 0;      // side of that larger mesh (0 = no plan)
   cufftHandle c2r = 0;        // Ng^3 C2R, batch = chunk
   bool c2r_ok = false;
   cufftHandle z2d = 0;        // Ng^3 Z2D, batch = chunk (grid info)
@@ -120,6 +140,12 @@ struct bsk_plan {
   int cic_nmesh = 0;                    // NmeshCIC the table was built for
   void* work = nullptr;                 // cuFFT work area shared by the plan's transforms
   size_t work_bytes = 0;
+  // shell streaming (used when the resident fields would exceed mem_budget)
+  int stream_C = 0;                     // shells per streamed chunk (0 = buffers not held)
+  bool stream_tc = false;               // buffers include the bf16 split
+  bsk::StreamBuf stream_f[3];           // FP32 [C][K] each
+  bsk::StreamBuf stream_split;          // bf16 hi [C][K] then lo [C][K]
+  int last_stream_C = 0;                // chunk of the last streamed measurement (0 = resident)
   int n_alloc() const { return (n + chunk - 1) / chunk * chunk; }  // shells rounded to batches
 };
 
@@ -131,6 +157,9 @@ struct bsk_triset {
   bsk::DeviceSchedule sched;
   int2* dups = nullptr;  // device (dst, src): repeated triangles copy the first occurrence
   int n_dups = 0;
+  std::vector<bsk::HostTriangle> u_tri;  // first occurrences, in order
+  std::vector<int> u_idx;                // their positions in the list
+  mutable std::map<int, std::vector<bsk::StreamGroup>> groups;  // per streaming chunk size
 };
 
 namespace bsk {
@@ -150,6 +179,9 @@ void launch_filter(const bsk_plan* p, const cufftComplex* spec, int s0, int ns,
 // Indicator (or |k|-weighted when kweight) spectra, complex128.
 void launch_filter_indicator(const bsk_plan* p, int s0, int ns, int kweight,
                              cufftDoubleComplex* out, cudaStream_t st);
+// In-place scale * w[qa] w[qb] w[qc] of an N^3 half spectrum (window deconvolution).
+void launch_window(int N, float scale, cufftComplex* spec, const float* axis_w, int num_sms,
+                   cudaStream_t st);
 // FP32 -> (bf16 hi, bf16 lo) split, n elements.
 void launch_split(const float* in, __nv_bfloat16* hi, __nv_bfloat16* lo, int64_t n,
                   cudaStream_t st);

@@ -40,7 +40,8 @@ struct Row {
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 }  // namespace
 
-void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSchedule& out) {
+void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSchedule& out,
+                    const std::vector<int>* map_index) {
   out.release();
   std::map<std::pair<int, int>, int> index;
   std::vector<Row> rows;
@@ -62,7 +63,7 @@ void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSc
     Row& R = rows[r];
     R.lmin = std::min(R.lmin, h.l);
     R.lmax = std::max(R.lmax, h.l);
-    R.cols.emplace_back(h.l, (int)t);
+    R.cols.emplace_back(h.l, map_index ? (*map_index)[t] : (int)t);
   }
   std::sort(rows.begin(), rows.end(), [](const Row& a, const Row& b) {
     if (a.lmax != b.lmax) return a.lmax < b.lmax;

@@ -104,6 +104,24 @@ __global__ void extract_kernel(int N, int Ng, float scale, const float2* __restr
   }
 }
 
+// spec[m] *= scale * w[qa] w[qb] w[qc] over an N^3 half spectrum (N/2+1 last axis).
+__global__ void window_kernel(int N, float scale, float2* __restrict__ spec,
+                              const float* __restrict__ axis_w) {
+  const int H = N / 2 + 1;
+  const int64_t Mh = (int64_t)N * N * H;
+  for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < Mh;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(m % H);
+    const int64_t r = m / H;
+    const int qb = fft_freq((int)(r % N), N), qa = fft_freq((int)(r / N), N);
+    const float f = scale * axis_w[qa + N / 2] * axis_w[qb + N / 2] * axis_w[c + N / 2];
+    float2 v = spec[m];
+    v.x *= f;
+    v.y *= f;
+    spec[m] = v;
+  }
+}
+
 __device__ __forceinline__ bool in_shell(uint16_t code, int s) {
   int first = code & 0xFF;
   int cnt = (code >> 8) + 1;
@@ -230,6 +248,14 @@ void launch_extract(const bsk_plan* p, const cufftComplex* fine, cufftComplex* c
   extract_kernel<<<grid_for(p->Mh, 256, p->num_sms * 16), 256, 0, st>>>(
       p->N, p->Ng, scale, reinterpret_cast<const float2*>(fine), reinterpret_cast<float2*>(coarse),
       axis_w);
+  BSK_CHECK_CUDA(cudaGetLastError());
+}
+
+void launch_window(int N, float scale, cufftComplex* spec, const float* axis_w, int num_sms,
+                   cudaStream_t st) {
+  const int64_t Mh = (int64_t)N * N * (N / 2 + 1);
+  window_kernel<<<grid_for(Mh, 256, num_sms * 16), 256, 0, st>>>(
+      N, scale, reinterpret_cast<float2*>(spec), axis_w);
   BSK_CHECK_CUDA(cudaGetLastError());
 }
 

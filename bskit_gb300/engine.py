@@ -85,6 +85,12 @@ class Plan:
         _lib.call("bsk_plan_query", self.handle, info)
         return int(info[_lib.INFO_FOOTPRINT])
 
+    def stream_chunk(self):
+        """Shells per chunk of the last measurement's shell streaming (0 = fields resident)."""
+        info = (ctypes.c_int64 * _lib.INFO_COUNT)()
+        _lib.call("bsk_plan_query", self.handle, info)
+        return int(info[_lib.INFO_STREAM])
+
     def mode_counts(self):
         out = np.zeros(self.n_shells, dtype=np.int64)
         _lib.call("bsk_shell_mode_counts", self.handle, out.ctypes.data)
@@ -106,6 +112,16 @@ class Plan:
             else:
                 _lib.call("bsk_paint", self.handle, int(slot), ctypes.c_void_p(m.data_ptr()),
                           _stream_ptr(stream))
+        return m
+
+    def paint_subbox(self, slot, mesh, multi, stream=None):
+        """r2c of the sub-box multi = (a, b, c) of a larger cubic float32 CUDA mesh whose side
+        is a multiple of this plan's Nmesh (the block starting at (a N, b N, c N))."""
+        m = self._as_mesh(mesh, full=True)
+        a, b, c = (int(v) for v in multi)
+        with torch.cuda.device(self.device):
+            _lib.call("bsk_paint_subbox", self.handle, int(slot), ctypes.c_void_p(m.data_ptr()),
+                      int(m.shape[0]), a, b, c, _stream_ptr(stream))
         return m
 
     def measure_b(self, tset, slots=(0, 0, 0), precision="bf16x3", out=None, stream=None):
@@ -175,12 +191,17 @@ class Plan:
         return out
 
     # ------------------------------------------------------------------ helpers
-    def _as_mesh(self, mesh):
+    def _as_mesh(self, mesh, full=False):
         if isinstance(mesh, np.ndarray):
             mesh = torch.from_numpy(np.ascontiguousarray(mesh, dtype=np.float32))
         if not isinstance(mesh, torch.Tensor):
             raise TypeError("mesh must be a numpy array or torch tensor")
-        if tuple(mesh.shape) != (self.nmesh,) * 3:
+        if full:
+            n = mesh.shape[0] if mesh.dim() == 3 else -1
+            if mesh.dim() != 3 or len(set(mesh.shape)) != 1 or n % self.nmesh:
+                raise ValueError("mesh shape %s is not a cube whose side is a multiple of "
+                                 "Nmesh=%d" % (tuple(mesh.shape), self.nmesh))
+        elif tuple(mesh.shape) != (self.nmesh,) * 3:
             raise ValueError("mesh shape %s does not match Nmesh=%d" % (tuple(mesh.shape),
                                                                           self.nmesh))
         return mesh.to(device=self.device, dtype=torch.float32).contiguous()
@@ -198,3 +219,21 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def compensate_cic(mesh, nmesh_cic, out=None, stream=None):
+    """CIC window deconvolution of a whole cubic float32 CUDA mesh assigned on an
+    nmesh_cic^3 grid (returns ``out``, a new tensor unless given; may be ``mesh``)."""
+    _require_cuda()
+    if not isinstance(mesh, torch.Tensor) or mesh.dim() != 3 or len(set(mesh.shape)) != 1:
+        raise ValueError("mesh must be a cubic torch tensor")
+    m = mesh.to(dtype=torch.float32).contiguous()
+    if not m.is_cuda:
+        m = m.cuda()
+    if out is None:
+        out = torch.empty_like(m)
+    with torch.cuda.device(m.device):
+        _lib.call("bsk_compensate_cic", int(m.shape[0]), int(nmesh_cic),
+                  ctypes.c_void_p(m.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                  _stream_ptr(stream))
+    return out

@@ -65,7 +65,8 @@ enum bsk_grid_mode {
 /* bsk_plan_query() fields */
 enum bsk_info {
   BSK_INFO_NMESH = 0, BSK_INFO_NGRID = 1, BSK_INFO_NSHELLS = 2, BSK_INFO_QMAX = 3,
-  BSK_INFO_FOOTPRINT = 4, BSK_INFO_CHUNK = 5, BSK_INFO_DEVICE = 6, BSK_INFO_COUNT = 8
+  BSK_INFO_FOOTPRINT = 4, BSK_INFO_CHUNK = 5, BSK_INFO_DEVICE = 6, BSK_INFO_STREAM = 7,
+  BSK_INFO_COUNT = 8
 };
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -78,11 +79,17 @@ int bsk_last_error(char* buf, size_t len);
  * Create a plan for an N^3 mesh in a periodic box of side L with n shells
  * [edges[2s], edges[2s+1]].  Builds the per-mode shell table on the device,
  * the exact per-shell mode counts and the cuFFT plans.
- * mem_budget: bytes of device memory the plan may hold (0 = no limit).  An
- * operation whose allocation would take the plan's footprint (BSK_INFO_FOOTPRINT)
- * above it fails with BSK_ERR_OOM before allocating and leaves the plan usable.
- * Like the reference, which holds every shell field of a measurement in memory,
- * the plan keeps all n shell fields of a slot resident.
+ * mem_budget: bytes of device memory the plan may hold (0 = no limit).  When
+ * the resident shell fields of a measurement (all n shells of each slot, plus
+ * their bf16 split) would take the plan's footprint (BSK_INFO_FOOTPRINT) above
+ * it, bsk_measure_b(_range) and bsk_gridinfo stream the fields instead: shells
+ * are cut into chunks of C (a multiple of BSK_INFO_CHUNK, as large as the budget
+ * allows), the triangles are grouped by the chunks of their three shells, and
+ * each group runs on the fields of at most three chunks, recomputed from the
+ * painted spectrum when a chunk is needed again.  BSK_INFO_STREAM reports the C
+ * of the last measurement (0 = resident).  Any other allocation that would
+ * exceed the budget, or a budget too small for one chunk, fails with
+ * BSK_ERR_OOM before allocating and leaves the plan usable.
  * Replaces: FFTBispectrum.__init__ bin set-up, bskit/main.py:1485-1595, and
  *           the k-mask closures of main.py:1848-1852 / 264-268 / 314-320.
  */
@@ -92,7 +99,8 @@ int bsk_plan_create(int nmesh, double box_size, int n_shells, const double* shel
 /* Release every device resource of the plan.  Replaces: object teardown. */
 int bsk_plan_destroy(bsk_plan* plan);
 
-/* info[BSK_INFO_COUNT] <- N, Ng, n, qmax, footprint bytes, shell chunk, device. */
+/* info[BSK_INFO_COUNT] <- N, Ng, n, qmax, footprint bytes, shell chunk, device,
+ * streaming chunk of the last measurement. */
 int bsk_plan_query(const bsk_plan* plan, int64_t* info);
 
 /*
@@ -127,6 +135,29 @@ int bsk_paint(bsk_plan* plan, int slot, const float* mesh, void* stream);
  *           mode='complex'), scripts/measure/measure_bs_fast.py:45-57, 218-223.
  */
 int bsk_paint_cic(bsk_plan* plan, int slot, const float* mesh, int nmesh_cic, void* stream);
+
+/*
+ * As bsk_paint for the sub-box (a, b, c) of a larger mesh: the plan's N^3 block
+ * whose first point is (a N, b N, c N) in the nmesh_full^3 float32 array `mesh`
+ * (nmesh_full a multiple of N).  The block is transformed where it lies (a
+ * strided R2C); nothing is copied out of the full mesh.
+ * Replaces: field_subbox_pm (bskit/main.py:83-147, a nearest-grid-point cut of
+ *           the sub-region) + the sub-box FFTBispectrum's _paint_meshes,
+ *           scripts/measure/measure_subbox_bs_fast.py:262-284.
+ */
+int bsk_paint_subbox(bsk_plan* plan, int slot, const float* mesh, int nmesh_full, int a, int b,
+                     int c, void* stream);
+
+/*
+ * CIC window deconvolution of a whole float32 nmesh^3 mesh assigned on an
+ * nmesh_cic^3 grid: out = c2r[ r2c(mesh) / N^3 / prod_c sqrt(1 - 2/3
+ * sin^2(pi q_c / nmesh_cic)) ] (out may equal mesh).  Used before sub-boxes are
+ * cut, as the reference compensates the full mesh first.  Creates and destroys
+ * its own cuFFT plans and temporary spectrum; returns after the work is done.
+ * Replaces: mesh.apply(CompensateCICShotnoiseNgrid, ...) + mesh.compute(mode=
+ *           'real'), scripts/measure/measure_subbox_bs_fast.py:45-57, 236-246.
+ */
+int bsk_compensate_cic(int nmesh, int nmesh_cic, const float* mesh, float* out, void* stream);
 
 /*
  * Unnormalised bispectrum of every triangle of `set`:

@@ -12,6 +12,8 @@ that numpy>=1.24 needs for ``bskit/main.py:1381``.  It then writes:
   main.py:1074/1121/1181) for a set of parameter combinations: full arrays
   for small lists, (shape, sha256 of the float64/int64 bytes, first/last rows)
   for large ones.
+* ``subbox_multiindex.json`` -- ``subbox_index_to_multiindex`` (main.py:54)
+  for every sub-box index at nsub_per_side = 1..4.
 * copies of the upstream golden grid-info outputs
   (``examples/tests/output_ref/Lbox1000_512_kf_3kf_3lowkbins*.dat``) and the
   first rows of the P(k) golden file that carry shell mode counts.
@@ -173,6 +175,12 @@ def main(ref_root):
 
     with open(os.path.join(HERE, "bins_reference.json"), "w") as f:
         json.dump(out, f, indent=0)
+
+    # subbox_index_to_multiindex (main.py:54) for every sub-box of nsub = 1..4
+    sub = {str(n): [ref.subbox_index_to_multiindex(i, n).tolist() for i in range(n ** 3)]
+           for n in (1, 2, 3, 4)}
+    with open(os.path.join(HERE, "subbox_multiindex.json"), "w") as f:
+        json.dump(sub, f)
 
     src = os.path.join(ref_root, "examples", "tests", "output_ref")
     for name in ("Lbox1000_512_kf_3kf_3lowkbins.dat", "Lbox1000_512_kf_3kf_3lowkbins_slow.dat",

@@ -5,10 +5,13 @@ Tolerances (stated per test):
 * k_mean: 1e-12 relative (FP64 fields and sums on both sides);
 * B: the GPU fields are FP32 (cuFFT C2R), the oracle's FP64.  For every bin we
   report rel = |B - B_o| / |B_o| and the conditioning-free
-  nrm = |B - B_o| / (L^6/N^3 * sum_x |I_i I_j I_l|).  fp64/fp32/bf16x3 must meet
-  nrm <= 2e-6 on every bin, rel <= 1e-5 on every bin whose value is at least 10%
-  of its absolute sum (|B_o| >= 0.1 * abs sum; below that a 1e-6 normalised error
-  is no longer a 1e-5 relative one), and a median rel <= 1e-5 over all bins;
+  nrm = |B - B_o| / (L^6/N^3 * sum_x |I_i I_j I_l|).  fp64/fp32 must meet
+  nrm <= 2e-6 on every bin and bf16x3 nrm <= 4e-6 (each bf16 hi + lo pair
+  represents its FP32 value to about 2^-18 relative, and on shells one k_f wide
+  an exact emulation of the three bf16 products already reaches 2.0e-6); all
+  three must meet rel <= 1e-5 on every bin whose value is at least 10% of its
+  absolute sum (|B_o| >= 0.1 * abs sum; below that a 1e-6 normalised error is
+  no longer a 1e-5 relative one), and a median rel <= 1e-5 over all bins;
   bf16 (one MMA term) must meet nrm <= 1e-3.
 """
 import numpy as np
@@ -53,7 +56,7 @@ def _check_b(b, bo, babs, prec):
     if prec == "bf16":
         assert nrm.max() <= 1e-3
     else:
-        assert nrm.max() <= 2e-6
+        assert nrm.max() <= (4e-6 if prec == "bf16x3" else 2e-6)
         assert np.median(rel) <= 1e-5
         if well.any():
             assert rel[well].max() <= 1e-5
@@ -289,6 +292,75 @@ def test_mem_budget_refuses_before_allocating(cuda):
     np.testing.assert_allclose(roomy.measure_b(roomy.triangles(tri)).cpu().numpy(), ref,
                                rtol=1e-12, atol=1e-12 * np.abs(ref).max())
     roomy.close()
+
+
+def _streaming_case():
+    # 30 shells of width k_f up to 31 k_f on a 64^3 mesh (native grid): 4 streamed chunks
+    n, box = 64, 100.0
+    kf = TWO_PI / box
+    kw = dict(kmin=kf, kmax=32 * kf, dk=kf)
+    return n, box, kw, B.generate_bin_edge_list(**kw)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16x3"])
+def test_shell_streaming_under_budget(cuda, prec):
+    n, box, kw, edges = _streaming_case()
+    d1 = synthetic.lognormal_mesh(n, box, seed=31)
+    d2 = synthetic.noisy_copy(d1, seed=32)
+    probe = Plan(n, box, edges)
+    probe.paint(0, torch.from_numpy(d1))
+    probe.paint(1, torch.from_numpy(d2))
+    base = probe.footprint()
+    k = probe.ngrid ** 3
+    probe.close()
+    # room for one 8-shell chunk of three FP32 fields (+ the bf16 split), not for the
+    # 30 shells (32 with the FFT-batch padding) of one slot resident
+    room = 8 * k * (16 if prec == "bf16x3" else 12) + (1 << 20)
+    plan = Plan(n, box, edges, mem_budget=base + room)
+    plan.paint(0, torch.from_numpy(d1))
+    plan.paint(1, torch.from_numpy(d2))
+    f = [O.shell_fields(O.spectrum(d), n, box, edges) for d in (d1, d2)]
+    for nf, slots in ((1, (0, 0, 0)), (2, (0, 0, 1))):
+        tri = B.generate_triangle_bin_list(num_fields=nf, return_indices=True, **kw)
+        b = plan.measure_b(plan.triangles(tri), slots=slots, precision=prec)
+        plan.sync_check()
+        assert plan.stream_chunk() == 8
+        fa, fb, fc = (f[0], f[0], f[0]) if nf == 1 else (f[0], f[0], f[1])
+        bo = O.triple_sums(fa, fb, fc, tri) * box ** 6 / n ** 3
+        _check_b(b.cpu().numpy(), bo, _abs_sums(fa, fb, fc, tri, box, n), prec)
+    assert plan.footprint() <= base + room
+    plan.close()
+
+
+def test_gridinfo_streaming_under_budget(cuda):
+    n, box, kw, edges = _streaming_case()
+    tri = B.generate_triangle_bin_list(return_indices=True, **kw)
+    full = Plan(n, box, edges)
+    ts = full.triangles(tri)
+    ntri0, kmean0 = (x.cpu().numpy() for x in full.gridinfo(ts))
+    base = full.footprint()
+    k = full.ngrid ** 3
+    full.close()
+    spec = 8 * k // n * (n // 2 + 1) * 16
+    # one 8-shell chunk of six FP64 fields, not the resident 2 x 32 shells
+    plan = Plan(n, box, edges, mem_budget=base + 8 * 6 * 8 * k + spec + (1 << 20))
+    ts = plan.triangles(tri)
+    ntri, kmean = (x.cpu().numpy() for x in plan.gridinfo(ts))
+    plan.sync_check()
+    assert plan.stream_chunk() == 8
+    assert np.array_equal(ntri, ntri0)
+    ok = ntri0 > 0
+    # the streamed groups sum the FP64 products in another order than the resident tiles
+    np.testing.assert_allclose(kmean[ok], kmean0[ok], rtol=1e-11)
+    assert np.isnan(kmean[~ok]).all()
+    plan.close()
+    # a budget below one chunk is refused before allocating
+    from bskit_gb300 import _lib
+    tight = Plan(n, box, edges, mem_budget=base + 4 * 6 * 8 * k)
+    with pytest.raises(_lib.BskError) as e:
+        tight.gridinfo(tight.triangles(tri))
+    assert e.value.code == _lib.BSK_ERR_OOM
+    tight.close()
 
 
 def test_cic_compensated_paint(cuda):
