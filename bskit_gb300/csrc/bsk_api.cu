@@ -411,7 +411,10 @@ void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int prec
   const bool tc = precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16;
   BSK_REQUIRE(tc || precision == BSK_PREC_FP32 || precision == BSK_PREC_FP64, BSK_ERR_ARG,
               "unknown precision " + std::to_string(precision));
-  if (tc) BSK_REQUIRE(k0 % 64 == 0, BSK_ERR_ARG, "tensor-core ranges must start at a multiple of 64");
+  if (tc)
+    BSK_REQUIRE(k0 % 128 == 0 && (k1 % 128 == 0 || k1 == p->K), BSK_ERR_ARG,
+                "tensor-core point ranges must start and end at multiples of 128 (or end at "
+                "the whole grid)");
   if (p->mem_budget) {
     // resident path: all shells of each slot (and the split of the third) stay on the device
     const size_t field_bytes = (size_t)p->n_alloc() * p->K * sizeof(float);

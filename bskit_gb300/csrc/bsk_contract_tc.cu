@@ -4,31 +4,32 @@
 //
 // One persistent CTA per SM walks work items (tile of 128 pair rows x nc <= 64
 // columns, K slice of SLICE points), slice-major so that the CTAs running at
-// the same time share field data in L2.  Per 64-point chunk:
-//   * warp 0 (one lane) TMA-loads into an SMEM ring (6 stages with one source
-//     tile, 4 with two) the bf16 hi and lo tiles of the column fields as one
-//     128-row operand (rows 0..63 hi, 64..127 lo; SWIZZLE_128B, K-major) and
-//     the FP32 tile(s) of the pair-factor shells (one tile when one range covers
-//     both factors of every row, as for auto spectra), each with only as many
-//     shell rows (16/32/48/64) as the tile uses;
-//   * warps 10..17 (2 per TMEM lane quadrant, one 32-point half each) read the
+// the same time share field data in L2.  Per 128-point pipeline stage:
+//   * warp 0 (one lane) TMA-loads into an SMEM ring (3 stages with one source
+//     tile, 2 with two) the bf16 hi and lo tiles of the column fields, per
+//     64-point K block as one 128-row operand (rows 0..63 hi, 64..127 lo;
+//     SWIZZLE_128B, K-major), and the FP32 tile(s) of the pair-factor shells
+//     (one tile when one range covers both factors of every row, as for auto
+//     spectra), each with only as many shell rows (16/32/48/64) as the tile uses;
+//   * warps 10..17 (2 per TMEM lane quadrant, one 64-point half each) read the
 //     row's F1_i, F2_j from SMEM, form P = F1_i*F2_j with packed f32x2
 //     arithmetic, split P = hi + lo (bf16 round-to-nearest) and store them with
-//     tcgen05.st into the 4-stage TMEM A-operand ring (lane = GEMM row);
+//     tcgen05.st into the 2-stage TMEM A-operand ring (lane = GEMM row);
 //   * warp 1 (one lane) issues, per 16-point K step, tcgen05.mma kind::f16 with
 //     A from TMEM and B from SMEM: hi x [Bhi; Blo] (N = 64 + nc: one MMA yields
 //     both hi*Bhi and hi*Blo) and, for bf16x3, lo x Bhi (N = nc).  The tensor
-//     core's FP32 accumulate truncates, so an accumulator is only ever fed
-//     ACC_CHUNKS chunks (16 MMAs) before it is handed over;
+//     core's FP32 accumulate truncates, so an accumulator is only ever fed one
+//     stage (16 MMAs) before it is handed over;
 //   * warps 2..9 (2 per lane quadrant, 32 columns each) drain each finished
 //     accumulator with tcgen05.ld (hi*B + lo*Bhi columns and hi*Blo columns),
 //     add it into per-thread FP32 registers (round-to-nearest), and at the end
 //     of the slice add the entries that are triangle bins into the FP64 output
 //     (atomics).
-// The MMAs' completion is committed to two mbarriers per chunk: one frees the
+// The MMAs' completion is committed to two mbarriers per stage: one frees the
 // SMEM stage for the TMA producer, one frees the TMEM A stage for the A-operand
-// warps; the SMEM ring runs deeper than the TMEM ring so that more loads are in
-// flight than A stages exist.  Every
+// warps.  Stages are 128 points long because the single MMA-issuing thread,
+// whose barrier waits and commits cost about as much as its MMAs, sets the pace:
+// longer stages spread that fixed cost over more tensor-core work.  Every
 // wait is bounded (globaltimer); on expiry the kernel records an error flag,
 // stops issuing work, drains its own MMAs and frees TMEM.
 #include <cuda.h>
@@ -38,27 +39,30 @@
 namespace bsk {
 namespace tc {
 
-constexpr int KCH = 64;                       // points per chunk
-constexpr int ACC_CHUNKS = 2;                 // chunks summed inside one TMEM accumulator
-constexpr int ASTAGES = 4;                    // TMEM A-operand ring
+constexpr int KCH = 128;                      // points per pipeline stage
+constexpr int KBLK = 64;                      // points per SWIZZLE_128B K block of the B operand
+constexpr int ACC_CHUNKS = 1;                 // stages summed inside one TMEM accumulator
+constexpr int ASTAGES = 2;                    // TMEM A-operand ring
 constexpr int NACC = 2;                       // TMEM accumulators
-constexpr int B_TILE = kMaxCols * 128;        // 8 KB: 64 rows x 64 bf16 (hi, then lo)
-constexpr int A_HALF = kMaxSrcRows * 128;     // 8 KB: 64 rows x 32 fp32
-constexpr int A_TILE = 2 * A_HALF;            // 16 KB
+constexpr int B_TILE = kMaxCols * 128;        // 8 KB: 64 rows x 64 bf16 (one K block, hi or lo)
+constexpr int B_BLOCK = 2 * B_TILE;           // 16 KB: hi then lo of one K block
+constexpr int A_QUARTER = kMaxSrcRows * 128;  // 8 KB: 64 rows x 32 fp32
+constexpr int A_TILE = 4 * A_QUARTER;         // 32 KB: one source tile of a stage
 constexpr int NUM_WARPS = 18;                 // producer, MMA, 8 drain, 8 A-operand
 constexpr int THREADS = NUM_WARPS * 32;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_COL = 0;               // accumulator b at 128 b: [0,64) hi*B+lo*Bhi, [64,128) hi*Blo
-constexpr uint32_t A_COL = 256;               // A stage s at 256 + 64 s: hi +0..31, lo +32..63
+constexpr uint32_t A_COL = 256;               // A stage a at 256 + 128 a: hi +0..63, lo +64..127
 constexpr int64_t SLICE = 16384;              // points per work item
 constexpr unsigned long long kTimeoutNs = 2000000000ull;
 
-// An SMEM stage holds B hi / lo (16 KB) + one or two FP32 source tiles (16 KB each).
+// An SMEM stage holds two K blocks of B hi / lo (32 KB) + one or two FP32 source
+// tiles (32 KB each).
 template <bool kTwoSrc> struct Ring {
-  static constexpr int kStageBytes = 2 * B_TILE + (kTwoSrc ? 2 : 1) * A_TILE;
-  static constexpr int kStages = kTwoSrc ? 4 : 6;
+  static constexpr int kStageBytes = 2 * B_BLOCK + (kTwoSrc ? 2 : 1) * A_TILE;
+  static constexpr int kStages = kTwoSrc ? 2 : 3;
 };
-constexpr int MAX_SSTAGES = 6;
+constexpr int MAX_SSTAGES = 3;
 
 struct Bars {
   uint64_t full[MAX_SSTAGES];      // TMA bytes landed
@@ -123,7 +127,7 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
 // is cheap; the clock is read every 16 polls and global memory (the shared
 // error flag, the wall clock) only about every 2^20 cycles, so that no memory
 // round trip sits between a barrier's completion and the waiter seeing it.
-__device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __noinline__ bool mbar_wait_slow(uint64_t* bar, uint32_t parity) {
   if (mbar_try(bar, parity)) return true;
   long long c0 = clock64();
   unsigned long long t0 = 0;
@@ -144,6 +148,12 @@ __device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
       }
     }
   }
+}
+// A phase that is already complete costs one try_wait inline; the polling loop is
+// out of line.  (A call per wait was a measurable share of the MMA thread's time.)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  return mbar_wait_slow(bar, parity);
 }
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint64_t* bar,
                                             int x, int y) {
@@ -315,10 +325,11 @@ __global__ void __launch_bounds__(THREADS, 1)
         const bool one_src = !kTwoSrc || (same_src && td.i0 == td.j0);
         const int64_t x_begin = k_begin + sl * SLICE;
         const int64_t x_end = min(k_end, x_begin + SLICE);
-        // bytes per chunk: the column rows of hi and lo, both halves of each source tile
+        // bytes per stage: the column rows of hi and lo in both K blocks, the four
+        // 32-point quarters of each source tile
         const uint32_t bytes =
-            (uint32_t)(2 * box_rows(td.nc) * 128 +
-                       2 * 128 * (box_rows(td.ni) + (one_src ? 0 : box_rows(td.nj))));
+            (uint32_t)(4 * box_rows(td.nc) * 128 +
+                       4 * 128 * (box_rows(td.ni) + (one_src ? 0 : box_rows(td.nj))));
         for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
           const int s = chunk % SST;
           const uint32_t ph = (chunk / SST) & 1;
@@ -326,15 +337,18 @@ __global__ void __launch_bounds__(THREADS, 1)
           mbar_arrive_tx(&bars->full[s], bytes);
           const uint32_t st = sbase + s * STAGE_BYTES;
           const int xi = (int)x;
-          load_rows(st, &maps.hi16, &maps.hi32, &maps.hi64, &bars->full[s], xi, td.l0, td.nc);
-          load_rows(st + B_TILE, &maps.lo16, &maps.lo32, &maps.lo64, &bars->full[s], xi, td.l0,
-                    td.nc);
-          for (int h = 0; h < 2; ++h) {
-            load_rows(st + 2 * B_TILE + h * A_HALF, &maps.f1_16, &maps.f1_32, &maps.f1_64,
-                      &bars->full[s], xi + 32 * h, td.i0, td.ni);
+          for (int kb = 0; kb < KCH / KBLK; ++kb) {
+            load_rows(st + kb * B_BLOCK, &maps.hi16, &maps.hi32, &maps.hi64, &bars->full[s],
+                      xi + KBLK * kb, td.l0, td.nc);
+            load_rows(st + kb * B_BLOCK + B_TILE, &maps.lo16, &maps.lo32, &maps.lo64,
+                      &bars->full[s], xi + KBLK * kb, td.l0, td.nc);
+          }
+          for (int q = 0; q < 4; ++q) {
+            load_rows(st + 2 * B_BLOCK + q * A_QUARTER, &maps.f1_16, &maps.f1_32, &maps.f1_64,
+                      &bars->full[s], xi + 32 * q, td.i0, td.ni);
             if (!one_src)
-              load_rows(st + 2 * B_TILE + A_TILE + h * A_HALF, &maps.f2_16, &maps.f2_32,
-                        &maps.f2_64, &bars->full[s], xi + 32 * h, td.j0, td.nj);
+              load_rows(st + 2 * B_BLOCK + A_TILE + q * A_QUARTER, &maps.f2_16, &maps.f2_32,
+                        &maps.f2_64, &bars->full[s], xi + 32 * q, td.j0, td.nj);
           }
         }
       }
@@ -371,11 +385,11 @@ __global__ void __launch_bounds__(THREADS, 1)
           if (!mbar_wait(&bars->afull[a], pa)) { ok = false; break; }
           tc_fence_after();
           const uint32_t st = sbase + s * STAGE_BYTES;
-          const uint32_t a_hi = tmem + A_COL + a * 64;
-          const uint32_t a_lo = a_hi + 32;
+          const uint32_t a_hi = tmem + A_COL + a * 128;
+          const uint32_t a_lo = a_hi + 64;
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const uint64_t bdesc = desc_sw128(st + 32 * k);
+          for (int k = 0; k < KCH / 16; ++k) {
+            const uint64_t bdesc = desc_sw128(st + (k >> 2) * B_BLOCK + 32 * (k & 3));
             mma_ts(d_tmem, a_hi + 8 * k, bdesc, idesc_stack, accum);
             if (terms >= 3) mma_ts(d_tmem, a_lo + 8 * k, bdesc, idesc_hi, 1);
             accum = 1;
@@ -449,7 +463,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   } else {
     // ------------------------------------------------------------ A-operand producers
     const int qd = warp & 3;
-    const int half = (warp - 10) >> 2;
+    const int half = (warp - 10) >> 2;  // points [64 half, 64 half + 64) of a stage
     const int r = qd * 32 + lane;
     const uint32_t tlane = (uint32_t)(qd * 32) << 16;
     uint32_t chunk = 0;
@@ -475,16 +489,18 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (!__all_sync(0xffffffffu, mbar_wait(&bars->aempty[a], pa ^ 1))) { ok = false; break; }
         tc_fence_after();
         const uint8_t* st = smem + s * STAGE_BYTES;
-        const uint8_t* row1 = st + 2 * B_TILE + half * A_HALF + pi * 128;
-        const uint8_t* row2 = st + 2 * B_TILE + src2 + half * A_HALF + pj * 128;
-        const uint32_t a_hi = tmem + tlane + A_COL + a * 64 + half * 16;
+        const uint32_t a_hi = tmem + tlane + A_COL + a * 128 + half * 32;
 #pragma unroll
-        for (int sub = 0; sub < 2; ++sub) {
+        for (int sub = 0; sub < 4; ++sub) {
+          // points 64 half + 16 sub .. +16: quarter 2 half + sub / 2 of the source tile
+          const int qoff = (2 * half + (sub >> 1)) * A_QUARTER;
+          const uint8_t* row1 = st + 2 * B_BLOCK + qoff + pi * 128;
+          const uint8_t* row2 = st + 2 * B_BLOCK + src2 + qoff + pj * 128;
           uint32_t hi[8], lo[8];
           if (valid) {
 #pragma unroll
             for (int c4 = 0; c4 < 4; ++c4) {
-              const int c = sub * 4 + c4;  // logical 16-B chunk (4 floats)
+              const int c = (sub & 1) * 4 + c4;  // logical 16-B chunk (4 floats) of the row
               const ulonglong2 va =
                   *reinterpret_cast<const ulonglong2*>(row1 + ((c ^ (pi & 7)) << 4));
               const ulonglong2 vb =
@@ -497,7 +513,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int e = 0; e < 8; ++e) hi[e] = lo[e] = 0u;
           }
           tmem_st8(a_hi + sub * 8, hi);
-          tmem_st8(a_hi + 32 + sub * 8, lo);
+          tmem_st8(a_hi + 64 + sub * 8, lo);
         }
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         tc_fence_before();
@@ -558,7 +574,9 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
                         int64_t K, int64_t k_begin, int64_t k_end, int terms, double* out,
                         int num_sms, cudaStream_t st) {
   if (s.n_tiles == 0 || k_end <= k_begin) return;
-  BSK_REQUIRE(k_begin % tc::KCH == 0, BSK_ERR_ARG, "k_begin must be a multiple of 64");
+  BSK_REQUIRE(k_begin % tc::KCH == 0, BSK_ERR_ARG, "k_begin must be a multiple of 128");
+  BSK_REQUIRE(k_end % tc::KCH == 0 || k_end == K, BSK_ERR_ARG,
+              "k_end must be a multiple of 128 or the whole grid");
   BSK_REQUIRE(K < (int64_t)1 << 31, BSK_ERR_UNSUPPORTED, "grid too large for 32-bit TMA x");
   BSK_REQUIRE(K % 8 == 0, BSK_ERR_UNSUPPORTED, "K must be a multiple of 8");
   tc::Maps m;

@@ -9,9 +9,9 @@ are summed with one all-reduce -- the only exchange of the path (T doubles).
 import torch
 
 
-def point_range(n_points, rank, world, align=64):
+def point_range(n_points, rank, world, align=128):
     """[k0, k1) of rank's share of n_points; interior bounds are multiples of ``align``
-    (the tensor-core path consumes 64-point chunks)."""
+    (the tensor-core path consumes 128-point stages)."""
     if world < 1 or not 0 <= rank < world:
         raise ValueError("bad rank/world")
 

@@ -178,7 +178,9 @@ int bsk_measure_b(bsk_plan* plan, const bsk_triset* set, int slot_a, int slot_b,
  * [k_begin, k_end) of the C-ordered Ng^3 grid (an x-slab when the bounds are
  * multiples of Ng^2): partial sums that add up, over a partition of
  * [0, Ng^3), to bsk_measure_b's result.  Each GPU of a slab-sharded job calls
- * this for its slab and the partial vectors are summed (all-reduce).
+ * this for its slab and the partial vectors are summed (all-reduce).  The
+ * tensor-core precisions need k_begin and k_end at multiples of 128 (k_end may
+ * also be Ng^3), their pipeline stage.
  * Replaces: the per-rank local sums of bskit's MPI slabs, main.py:1875-1879.
  */
 int bsk_measure_b_range(bsk_plan* plan, const bsk_triset* set, int slot_a, int slot_b,

@@ -259,7 +259,7 @@ def test_slab_ranges_sum_to_whole(cuda):
     slab = plan.ngrid ** 2
     for prec in ("fp64", "bf16x3"):
         whole = plan.measure_b(ts, precision=prec).cpu().numpy()
-        cut = (plan.ngrid // 3) * slab // 64 * 64
+        cut = (plan.ngrid // 3) * slab // 128 * 128
         parts = [plan.measure_b_range(ts, 0, cut, precision=prec),
                  plan.measure_b_range(ts, cut, K, precision=prec)]
         tot = sum(p.cpu().numpy() for p in parts)

@@ -18,7 +18,7 @@ def test_point_range_partition():
             assert cuts[0][0] == 0 and cuts[-1][1] == n
             for (a0, a1), (b0, b1) in zip(cuts, cuts[1:]):
                 assert a1 == b0 and a0 <= a1
-            assert all(c[0] % 64 == 0 for c in cuts)
+            assert all(c[0] % 128 == 0 for c in cuts)
 
 
 class _FakePlan(object):
