@@ -189,9 +189,12 @@ void ensure_split(bsk_plan* p, int s, cudaStream_t st) {
   ensure_fields(p, s, st);
   if (f.split_ok) return;
   size_t n = (size_t)p->n_alloc() * p->K;
-  if (!f.hi) check_budget(p, n * 2 * sizeof(__nv_bfloat16), "the bf16 split of the fields");
-  if (!f.hi) f.hi = (__nv_bfloat16*)dmalloc(n * sizeof(__nv_bfloat16));
-  if (!f.lo) f.lo = (__nv_bfloat16*)dmalloc(n * sizeof(__nv_bfloat16));
+  if (!f.hi) {
+    // hi and lo are two planes of one allocation (the contraction loads both with one copy)
+    check_budget(p, n * 2 * sizeof(__nv_bfloat16), "the bf16 split of the fields");
+    f.hi = (__nv_bfloat16*)dmalloc(2 * n * sizeof(__nv_bfloat16));
+    f.lo = f.hi + n;
+  }
   launch_split(f.fields, f.hi, f.lo, (int64_t)n, st);
   f.split_ok = true;
 }
@@ -199,8 +202,7 @@ void ensure_split(bsk_plan* p, int s, cudaStream_t st) {
 void free_slot(FieldSlot& f) {
   if (f.spec) cudaFree(f.spec);
   if (f.fields) cudaFree(f.fields);
-  if (f.hi) cudaFree(f.hi);
-  if (f.lo) cudaFree(f.lo);
+  if (f.hi) cudaFree(f.hi);  // lo is the second plane of the same allocation
   f = FieldSlot{};
 }
 
@@ -890,13 +892,12 @@ int bsk_contract(bsk_plan* p, const bsk_triset* set, const float* f1, const floa
     __nv_bfloat16 *hi = nullptr, *lo = nullptr;
     if (precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16) {
       size_t n = (size_t)p->n * K;
-      hi = (__nv_bfloat16*)dmalloc_async(n * sizeof(__nv_bfloat16), st);
-      lo = (__nv_bfloat16*)dmalloc_async(n * sizeof(__nv_bfloat16), st);
+      hi = (__nv_bfloat16*)dmalloc_async(2 * n * sizeof(__nv_bfloat16), st);
+      lo = hi + n;
       launch_split(f3, hi, lo, (int64_t)n, st);
     }
     contract_dispatch(p, set, f1, f2, f3, hi, lo, K, 0, K, precision, out, st);
     if (hi) BSK_CHECK_CUDA(cudaFreeAsync(hi, st));
-    if (lo) BSK_CHECK_CUDA(cudaFreeAsync(lo, st));
   });
 }
 

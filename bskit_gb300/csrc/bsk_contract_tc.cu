@@ -80,9 +80,14 @@ constexpr int smem_bytes() {
   return Ring<kTwoSrc>::kStages * Ring<kTwoSrc>::kStageBytes + 1024 /*bars*/ + 1024 /*align*/;
 }
 
-// Tensor maps of one launch: bf16 column fields and FP32 sources, 16/32/64-row boxes.
+// Tensor maps of one launch: bf16 column fields and FP32 sources, 16/32/64-row boxes
+// (2D, one 64- or 32-point block per copy), and the one-copy-per-stage views used
+// when the grid is a multiple of 128 points: B as {64 points, shell, hi/lo plane,
+// 64-point block} with box {64, nc, 2, 2}; sources as {32 points, shell, 32-point
+// block} with box {32, rows, 4}.
 struct Maps {
   CUtensorMap hi16, hi32, hi64, lo16, lo32, lo64, f1_16, f1_32, f1_64, f2_16, f2_32, f2_64;
+  CUtensorMap b16, b32, b48, b64, a1_16, a1_32, a1_48, a1_64, a2_16, a2_32, a2_48, a2_64;
 };
 
 __device__ int g_tc_error;  // 0 ok, 1 a bounded wait expired
@@ -162,6 +167,28 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y, int z, int w) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ const CUtensorMap* by_rows(int n, const CUtensorMap* m16,
+                                                      const CUtensorMap* m32,
+                                                      const CUtensorMap* m48,
+                                                      const CUtensorMap* m64) {
+  return n > 48 ? m64 : n > 32 ? m48 : n > 16 ? m32 : m16;
 }
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -271,7 +298,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     contract_tc_kernel(const __grid_constant__ Maps maps, const TileDesc* __restrict__ tiles,
                        const int16_t* __restrict__ row_i, const int16_t* __restrict__ row_j,
                        const int32_t* __restrict__ map, int n_tiles, int same_src,
-                       int64_t k_begin, int64_t k_end, int64_t n_items, int terms,
+                       int64_t k_begin, int64_t k_end, int64_t n_items, int terms, int fused,
                        double* __restrict__ out) {
   constexpr int STAGE_BYTES = Ring<kTwoSrc>::kStageBytes;
   constexpr int SST = Ring<kTwoSrc>::kStages;
@@ -337,18 +364,32 @@ __global__ void __launch_bounds__(THREADS, 1)
           mbar_arrive_tx(&bars->full[s], bytes);
           const uint32_t st = sbase + s * STAGE_BYTES;
           const int xi = (int)x;
-          for (int kb = 0; kb < KCH / KBLK; ++kb) {
-            load_rows(st + kb * B_BLOCK, &maps.hi16, &maps.hi32, &maps.hi64, &bars->full[s],
-                      xi + KBLK * kb, td.l0, td.nc);
-            load_rows(st + kb * B_BLOCK + B_TILE, &maps.lo16, &maps.lo32, &maps.lo64,
-                      &bars->full[s], xi + KBLK * kb, td.l0, td.nc);
-          }
-          for (int q = 0; q < 4; ++q) {
-            load_rows(st + 2 * B_BLOCK + q * A_QUARTER, &maps.f1_16, &maps.f1_32, &maps.f1_64,
-                      &bars->full[s], xi + 32 * q, td.i0, td.ni);
+          if (fused) {
+            // one copy for B (both 64-point blocks, hi and lo: [block][plane][nc rows]),
+            // one per source tile ([32-point block][rows])
+            tma_load_4d(st, by_rows(td.nc, &maps.b16, &maps.b32, &maps.b48, &maps.b64),
+                        &bars->full[s], 0, td.l0, 0, xi / KBLK);
+            tma_load_3d(st + 2 * B_BLOCK,
+                        by_rows(td.ni, &maps.a1_16, &maps.a1_32, &maps.a1_48, &maps.a1_64),
+                        &bars->full[s], 0, td.i0, xi / 32);
             if (!one_src)
-              load_rows(st + 2 * B_BLOCK + A_TILE + q * A_QUARTER, &maps.f2_16, &maps.f2_32,
-                        &maps.f2_64, &bars->full[s], xi + 32 * q, td.j0, td.nj);
+              tma_load_3d(st + 2 * B_BLOCK + 4 * 128 * box_rows(td.ni),
+                          by_rows(td.nj, &maps.a2_16, &maps.a2_32, &maps.a2_48, &maps.a2_64),
+                          &bars->full[s], 0, td.j0, xi / 32);
+          } else {
+            for (int kb = 0; kb < KCH / KBLK; ++kb) {
+              load_rows(st + kb * B_BLOCK, &maps.hi16, &maps.hi32, &maps.hi64, &bars->full[s],
+                        xi + KBLK * kb, td.l0, td.nc);
+              load_rows(st + kb * B_BLOCK + B_TILE, &maps.lo16, &maps.lo32, &maps.lo64,
+                        &bars->full[s], xi + KBLK * kb, td.l0, td.nc);
+            }
+            for (int q = 0; q < 4; ++q) {
+              load_rows(st + 2 * B_BLOCK + q * A_QUARTER, &maps.f1_16, &maps.f1_32, &maps.f1_64,
+                        &bars->full[s], xi + 32 * q, td.i0, td.ni);
+              if (!one_src)
+                load_rows(st + 2 * B_BLOCK + A_TILE + q * A_QUARTER, &maps.f2_16, &maps.f2_32,
+                          &maps.f2_64, &bars->full[s], xi + 32 * q, td.j0, td.nj);
+            }
           }
         }
       }
@@ -363,9 +404,12 @@ __global__ void __launch_bounds__(THREADS, 1)
         const TileDesc td = tiles[item % n_tiles];
         const int64_t x_begin = k_begin + sl * SLICE;
         const int64_t x_end = min(k_end, x_begin + SLICE);
-        // hi x [Bhi; Blo] (rows nc..63 of the hi block are not loaded: their
-        // accumulator columns are never read), lo x Bhi
-        const uint32_t idesc_stack = idesc_bf16(terms >= 3 ? 64 + td.nc : td.nc);
+        // hi x [Bhi; Blo] (with 2D copies rows nc..63 of the hi block are not loaded:
+        // their accumulator columns are never read), lo x Bhi
+        // the lo rows of B sit right after the nc hi rows (one-copy loads) or 64 rows after
+        const int lo_row = fused ? td.nc : 64;
+        const uint32_t kb_bytes = fused ? 2u * td.nc * 128u : (uint32_t)B_BLOCK;
+        const uint32_t idesc_stack = idesc_bf16(terms >= 3 ? lo_row + td.nc : td.nc);
         const uint32_t idesc_hi = idesc_bf16(td.nc);
         int in_grp = 0;
         uint32_t d_tmem = 0, b = 0, accum = 0;
@@ -389,7 +433,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           const uint32_t a_lo = a_hi + 64;
 #pragma unroll
           for (int k = 0; k < KCH / 16; ++k) {
-            const uint64_t bdesc = desc_sw128(st + (k >> 2) * B_BLOCK + 32 * (k & 3));
+            const uint64_t bdesc = desc_sw128(st + (k >> 2) * kb_bytes + 32 * (k & 3));
             mma_ts(d_tmem, a_hi + 8 * k, bdesc, idesc_stack, accum);
             if (terms >= 3) mma_ts(d_tmem, a_lo + 8 * k, bdesc, idesc_hi, 1);
             accum = 1;
@@ -440,7 +484,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
             for (int e = 0; e < 16; ++e) acc[cc * 16 + e] += __uint_as_float(v[e]);
             if (terms >= 3) {
-              tmem_ld16(taddr + ACC_COL + b * 128 + 64 + cc * 16, v);
+              tmem_ld16(taddr + ACC_COL + b * 128 + (fused ? td.nc : 64) + cc * 16, v);
 #pragma unroll
               for (int e = 0; e < 16; ++e) acc[cc * 16 + e] += __uint_as_float(v[e]);
             }
@@ -479,7 +523,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       const bool valid = ri >= 0;
       const int pi = valid ? ri - td.i0 : 0;
       const int pj = valid ? rj - td.j0 : 0;
-      const int src2 = one_src ? 0 : A_TILE;
+      // source tiles: [32-point quarter][rows] with the quarter stride of the copy
+      const int qstride = fused ? box_rows(td.ni) * 128 : A_QUARTER;
+      const int src2 = one_src ? 0 : (fused ? 4 * qstride : A_TILE);
+      const int qstride2 = one_src ? qstride : (fused ? box_rows(td.nj) * 128 : A_QUARTER);
       for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
         const int s = chunk % SST;
         const uint32_t ph = (chunk / SST) & 1;
@@ -493,9 +540,9 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
         for (int sub = 0; sub < 4; ++sub) {
           // points 64 half + 16 sub .. +16: quarter 2 half + sub / 2 of the source tile
-          const int qoff = (2 * half + (sub >> 1)) * A_QUARTER;
-          const uint8_t* row1 = st + 2 * B_BLOCK + qoff + pi * 128;
-          const uint8_t* row2 = st + 2 * B_BLOCK + src2 + qoff + pj * 128;
+          const int qq = 2 * half + (sub >> 1);
+          const uint8_t* row1 = st + 2 * B_BLOCK + qq * qstride + pi * 128;
+          const uint8_t* row2 = st + 2 * B_BLOCK + src2 + qq * qstride2 + pj * 128;
           uint32_t hi[8], lo[8];
           if (valid) {
 #pragma unroll
@@ -567,6 +614,35 @@ void make_map(CUtensorMap* m, CUtensorMapDataType dt, int esize, const void* bas
               "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
+// View of a [rows][K] array with K cut into blocks of `blk` points:
+// dims {blk, rows, (planes,) K / blk}; box {blk, box_rows, (2,) nblk}.  Returns false
+// (map unusable) instead of failing when the driver rejects the layout.
+bool make_block_map(CUtensorMap* m, CUtensorMapDataType dt, int esize, const void* base,
+                    int64_t K, int rows, int blk, int box_rows, int nblk, int64_t plane_bytes) {
+  const bool planes = plane_bytes > 0;
+  cuuint64_t dims[4], strides[3];
+  cuuint32_t box[4], estr[4] = {1, 1, 1, 1};
+  int rank;
+  if (planes) {
+    rank = 4;
+    dims[0] = (cuuint64_t)blk; dims[1] = (cuuint64_t)rows; dims[2] = 2;
+    dims[3] = (cuuint64_t)(K / blk);
+    strides[0] = (cuuint64_t)K * esize; strides[1] = (cuuint64_t)plane_bytes;
+    strides[2] = (cuuint64_t)blk * esize;
+    box[0] = blk; box[1] = box_rows; box[2] = 2; box[3] = nblk;
+  } else {
+    rank = 3;
+    dims[0] = (cuuint64_t)blk; dims[1] = (cuuint64_t)rows; dims[2] = (cuuint64_t)(K / blk);
+    strides[0] = (cuuint64_t)K * esize; strides[1] = (cuuint64_t)blk * esize;
+    box[0] = blk; box[1] = box_rows; box[2] = nblk;
+  }
+  CUresult r = encode_fn()(m, dt, rank, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 }  // namespace tc
 
 void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f2,
@@ -594,6 +670,20 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
   tc::make_map(&m.f2_16, F32, 4, f2, K, n_shells, 32, 16);
   tc::make_map(&m.f2_32, F32, 4, f2, K, n_shells, 32, 32);
   tc::make_map(&m.f2_64, F32, 4, f2, K, n_shells, 32, 64);
+  // One copy per stage for B and per source tile when K is a multiple of the stage and
+  // hi / lo are two planes of one allocation (lo above hi, 16-byte multiple apart).
+  const int64_t plane = (int64_t)((const char*)f3_lo - (const char*)f3_hi);
+  bool fused = K % tc::KCH == 0 && plane > 0 && plane % 16 == 0;
+  const int rows16[4] = {16, 32, 48, 64};
+  CUtensorMap* bmaps[4] = {&m.b16, &m.b32, &m.b48, &m.b64};
+  CUtensorMap* a1maps[4] = {&m.a1_16, &m.a1_32, &m.a1_48, &m.a1_64};
+  CUtensorMap* a2maps[4] = {&m.a2_16, &m.a2_32, &m.a2_48, &m.a2_64};
+  for (int i = 0; i < 4 && fused; ++i) {
+    fused = tc::make_block_map(bmaps[i], BF, 2, f3_hi, K, n_shells, tc::KBLK, rows16[i],
+                               tc::KCH / tc::KBLK, plane) &&
+            tc::make_block_map(a1maps[i], F32, 4, f1, K, n_shells, 32, rows16[i], 4, 0) &&
+            tc::make_block_map(a2maps[i], F32, 4, f2, K, n_shells, 32, rows16[i], 4, 0);
+  }
   bool two_src = f1 != f2;
   for (const TileDesc& d : s.h_tiles) two_src = two_src || d.i0 != d.j0;
   constexpr int kMaxDev = 64;
@@ -613,7 +703,7 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
   if (grid > n_items) grid = n_items;
   kern<<<(unsigned)grid, tc::THREADS, smem, st>>>(
       m, s.tiles, s.row_i, s.row_j, s.map, s.n_tiles, f1 == f2 ? 1 : 0, k_begin, k_end,
-      n_items, terms, out);
+      n_items, terms, fused ? 1 : 0, out);
   BSK_CHECK_CUDA(cudaGetLastError());
 }
 
