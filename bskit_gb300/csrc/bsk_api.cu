@@ -137,6 +137,7 @@ int64_t footprint(const bsk_plan* p) {
     if (s.hi) fp += (int64_t)p->n_alloc() * p->K * 4;
   }
   if (p->stream_C) fp += (int64_t)p->stream_C * p->K * (3 * 4 + (p->stream_tc ? 4 : 0));
+  if (p->synth_ws) fp += (int64_t)p->synth_ws_bytes;
   return fp + (int64_t)p->work_bytes;
 }
 
@@ -161,14 +162,52 @@ void release_stream(bsk_plan* p) {
   p->stream_tc = false;
 }
 
-// Masked shell fields of `slot` for every shell: filter kernel + batched C2R.
-void ensure_fields(bsk_plan* p, int s, cudaStream_t st) {
+void alloc_split(bsk_plan* p, FieldSlot& f) {
+  if (f.hi) return;
+  // hi and lo are two planes of one allocation (the contraction loads both with one copy)
+  const size_t n = (size_t)p->n_alloc() * p->K;
+  check_budget(p, n * 2 * sizeof(__nv_bfloat16), "the bf16 split of the fields");
+  f.hi = (__nv_bfloat16*)dmalloc(2 * n * sizeof(__nv_bfloat16));
+  f.lo = f.hi + n;
+  // shells beyond n (padding to the FFT batch) are read by some tiles' boxes: keep them zero
+  const size_t pad = (size_t)(p->n_alloc() - p->n) * p->K;
+  if (pad) {
+    BSK_CHECK_CUDA(cudaMemset(f.hi + (size_t)p->n * p->K, 0, pad * sizeof(__nv_bfloat16)));
+    BSK_CHECK_CUDA(cudaMemset(f.lo + (size_t)p->n * p->K, 0, pad * sizeof(__nv_bfloat16)));
+  }
+}
+
+// Masked shell fields of `slot` for every shell.  With a grid the field synthesis
+// supports, its pruned FFT passes write the fields (and, when `with_split`, their bf16
+// hi / lo planes in the same pass); otherwise filter kernel + batched cuFFT C2R.
+void ensure_fields(bsk_plan* p, int s, cudaStream_t st, bool with_split = false) {
   FieldSlot& f = p->slot[s];
   BSK_REQUIRE(f.painted, BSK_ERR_STATE, "field slot " + std::to_string(s) + " was not painted");
   if (f.fields_ok) return;
   if (!f.fields) {
     check_budget(p, (size_t)p->n_alloc() * p->K * sizeof(float), "the shell fields");
     f.fields = (float*)dmalloc((size_t)p->n_alloc() * p->K * sizeof(float));
+    const size_t pad = (size_t)(p->n_alloc() - p->n) * p->K;
+    if (pad)
+      BSK_CHECK_CUDA(cudaMemset(f.fields + (size_t)p->n * p->K, 0, pad * sizeof(float)));
+  }
+  if (p->use_synth) {
+    if (!p->synth_ws) {
+      check_budget(p, p->synth_ws_bytes, "the field-synthesis workspace");
+      p->synth_ws = dmalloc(p->synth_ws_bytes);
+      synth_init_workspace(p->Ng, p->synth_ws);
+    }
+    if (with_split) alloc_split(p, f);
+    for (int s0 = 0; s0 < p->n; s0 += p->chunk) {
+      const int ns = std::min(p->chunk, p->n - s0);
+      int R = 0;
+      for (int k = s0; k < s0 + ns; ++k) R = std::max(R, p->shell_r[k]);
+      launch_synth(p->Ng, f.spec, p->table, s0, ns, R, p->synth_ws, f.fields,
+                   with_split ? f.hi : nullptr, with_split ? f.lo : nullptr, st);
+    }
+    f.fields_ok = true;
+    f.split_ok = with_split;
+    return;
   }
   bind_work(p, p->c2r, st);
   for (int s0 = 0; s0 < p->n; s0 += p->chunk) {
@@ -186,15 +225,10 @@ void ensure_fields(bsk_plan* p, int s, cudaStream_t st) {
 
 void ensure_split(bsk_plan* p, int s, cudaStream_t st) {
   FieldSlot& f = p->slot[s];
-  ensure_fields(p, s, st);
+  ensure_fields(p, s, st, true);
   if (f.split_ok) return;
-  size_t n = (size_t)p->n_alloc() * p->K;
-  if (!f.hi) {
-    // hi and lo are two planes of one allocation (the contraction loads both with one copy)
-    check_budget(p, n * 2 * sizeof(__nv_bfloat16), "the bf16 split of the fields");
-    f.hi = (__nv_bfloat16*)dmalloc(2 * n * sizeof(__nv_bfloat16));
-    f.lo = f.hi + n;
-  }
+  alloc_split(p, f);
+  const size_t n = (size_t)p->n_alloc() * p->K;
   launch_split(f.fields, f.hi, f.lo, (int64_t)n, st);
   f.split_ok = true;
 }
@@ -220,6 +254,7 @@ void destroy_plan(bsk_plan* p) {
   if (p->c2r_ok) cufftDestroy(p->c2r);
   if (p->z2d_ok) cufftDestroy(p->z2d);
   if (p->work) cudaFree(p->work);
+  if (p->synth_ws) cudaFree(p->synth_ws);
   release_stream(p);
   delete p;
 }
@@ -438,6 +473,7 @@ void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int prec
     release_stream(p);
   }
   p->last_stream_C = 0;
+  if (tc) ensure_split(p, c, st);  // first, so that a synthesis pass writes the split as well
   ensure_fields(p, a, st);
   ensure_fields(p, b, st);
   ensure_fields(p, c, st);
@@ -620,6 +656,14 @@ int bsk_plan_create(int nmesh, double box_size, int n_shells, const double* shel
                 "internal: shell mode beyond the reduced-grid bound");
     p->counts.assign(hc.begin(), hc.end());
 
+    p->shell_r.resize(n_shells);
+    for (int s = 0; s < n_shells; ++s) {
+      const double hi = p->edges[2 * s + 1];
+      const double q = hi >= p->edges[2 * s] ? std::floor(hi / kf * (1.0 + 1e-9)) : 0.0;
+      p->shell_r[s] = (int)std::min<double>(std::max(q, 0.0), qmax);
+    }
+    p->use_synth = synth_supported(p->Ng);
+    if (p->use_synth) p->synth_ws_bytes = synth_workspace_bytes(p->Ng, qmax, p->chunk);
     make_r2c(p.get());
     make_c2r(p.get());
     p->chunk_spec = (cufftComplex*)dmalloc((size_t)p->chunk * p->Mh * sizeof(cufftComplex));

@@ -146,6 +146,11 @@ struct bsk_plan {
   bsk::StreamBuf stream_f[3];           // FP32 [C][K] each
   bsk::StreamBuf stream_split;          // bf16 hi [C][K] then lo [C][K]
   int last_stream_C = 0;                // chunk of the last streamed measurement (0 = resident)
+  // field synthesis (pruned FFT passes) instead of filter + cuFFT C2R
+  bool use_synth = false;
+  std::vector<int> shell_r;             // largest |q_c| of a mode in each shell
+  void* synth_ws = nullptr;             // twiddles + X / Y pass intermediates of one batch
+  size_t synth_ws_bytes = 0;
   int n_alloc() const { return (n + chunk - 1) / chunk * chunk; }  // shells rounded to batches
 };
 
@@ -182,6 +187,15 @@ void launch_filter_indicator(const bsk_plan* p, int s0, int ns, int kweight,
 // In-place scale * w[qa] w[qb] w[qc] of an N^3 half spectrum (window deconvolution).
 void launch_window(int N, float scale, cufftComplex* spec, const float* axis_w, int num_sms,
                    cudaStream_t st);
+// Field synthesis: fields (and optionally the hi / lo planes) of shells [s0, s0 + ns)
+// from the slot spectrum by three pruned FFT passes; R = largest |q_c| of those shells.
+bool synth_supported(int n);
+size_t synth_workspace_bytes(int n, int max_r, int batch);
+// Twiddle table at the start of the workspace (synchronous; once, after allocation).
+void synth_init_workspace(int n, void* work);
+void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0, int ns, int R,
+                  void* work, float* fields, __nv_bfloat16* hi, __nv_bfloat16* lo,
+                  cudaStream_t st);
 // FP32 -> (bf16 hi, bf16 lo) split, n elements.
 void launch_split(const float* in, __nv_bfloat16* hi, __nv_bfloat16* lo, int64_t n,
                   cudaStream_t st);

@@ -1,0 +1,456 @@
+// Shell-field synthesis: I_s(x) = c2r[ dhat_k 1{k in shell s} ] for a batch of shells,
+// as three pruned passes of length-Ng inverse FFTs written for this problem.
+//
+// A shell of radius r occupies |q_a|, |q_b|, q_c <= r of the half spectrum, so:
+//   X pass: for every column (q_b, q_c) with |q_b|, q_c <= r, the masked spectrum along
+//           q_a (only |q_a| <= r nonzero) -> G[s][x][q_b][q_c]   (reads the slot spectrum
+//           and the shell table once for all shells of the batch);
+//   Y pass: for every (x, q_c <= r), G along q_b -> Hh[s][x][y][q_c];
+//   Z pass: for every two rows (x, y), (x, y+1), the Hermitian-extended sequences along
+//           q_c packed as Z1 + i Z2 -> one complex inverse FFT whose real and imaginary
+//           parts are the two real output rows; the rows are written as FP32 fields and,
+//           when asked, as the bf16 hi / lo planes of the tensor-core contraction.
+// Every array keeps q_c fastest, so each pass reads and writes 16-wide (128-byte) runs.
+// The FFTs are radix-8/4/2/3/5 Stockham passes in shared memory (twiddles from a table
+// computed in double precision on the host); unnormalised, sign +1, as cuFFT's C2R.
+#include <cmath>
+
+#include "bsk_internal.cuh"
+
+namespace bsk {
+namespace {
+
+constexpr int kLines = 16;  // lines (one 16-wide q_c run) per block
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int fft_freq(int a, int n) { return a < (n + 1) / 2 ? a : a - n; }
+
+__device__ __forceinline__ bool in_shell(uint16_t code, int s) {
+  const int first = code & 0xFF;
+  const int cnt = (code >> 8) + 1;
+  return first != 0xFF && s >= first && s < first + cnt;
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// multiply by +i
+__device__ __forceinline__ float2 mul_i(float2 a) { return make_float2(-a.y, a.x); }
+
+// Unnormalised R-point DFT with sign +1 in registers: v[q] <- sum_r v[r] e^{+2 pi i r q / R}.
+// roots[R][k] = e^{+2 pi i k / R}.
+__device__ __forceinline__ void dft2(float2* v) {
+  const float2 a = v[0], b = v[1];
+  v[0] = cadd(a, b);
+  v[1] = csub(a, b);
+}
+__device__ __forceinline__ void dft4(float2* v) {
+  const float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+  const float2 s13 = cadd(v[1], v[3]), d13 = mul_i(csub(v[1], v[3]));
+  v[0] = cadd(s02, s13);
+  v[2] = csub(s02, s13);
+  v[1] = cadd(d02, d13);
+  v[3] = csub(d02, d13);
+}
+__device__ __forceinline__ void dft8(float2* v) {
+  // two 4-point DFTs of the even and odd samples, combined with e^{+2 pi i k / 8}
+  float2 e[4] = {v[0], v[2], v[4], v[6]};
+  float2 o[4] = {v[1], v[3], v[5], v[7]};
+  dft4(e);
+  dft4(o);
+  const float h = 0.70710678118654752f;
+  const float2 w1 = make_float2(h, h), w3 = make_float2(-h, h);
+  const float2 t0 = o[0], t1 = cmul(o[1], w1), t2 = mul_i(o[2]), t3 = cmul(o[3], w3);
+  v[0] = cadd(e[0], t0);
+  v[4] = csub(e[0], t0);
+  v[1] = cadd(e[1], t1);
+  v[5] = csub(e[1], t1);
+  v[2] = cadd(e[2], t2);
+  v[6] = csub(e[2], t2);
+  v[3] = cadd(e[3], t3);
+  v[7] = csub(e[3], t3);
+}
+template <int R>
+__device__ __forceinline__ void dft_generic(float2* v, const float2* roots) {
+  float2 out[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    float2 acc = v[0];
+#pragma unroll
+    for (int r = 1; r < R; ++r) acc = cadd(acc, cmul(v[r], roots[(r * q) % R]));
+    out[q] = acc;
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q) v[q] = out[q];
+}
+
+struct FftPlan {
+  int n;
+  int np;
+  int radix[8];
+  float2 root3[3];
+  float2 root5[5];
+};
+
+// Radix plan of a length: 8s, then a 4 and a 2, then 3s and 5s (constexpr, so that a
+// compile-time length gets a fully unrolled pass sequence).
+__host__ __device__ constexpr int plan_np(int n) {
+  int np = 0;
+  while (n % 8 == 0) { n /= 8; ++np; }
+  if (n % 4 == 0) { n /= 4; ++np; }
+  if (n % 2 == 0) { n /= 2; ++np; }
+  while (n % 3 == 0) { n /= 3; ++np; }
+  while (n % 5 == 0) { n /= 5; ++np; }
+  return n == 1 ? np : -1;
+}
+__host__ __device__ constexpr int plan_radix(int n, int p) {
+  int k = 0;
+  while (n % 8 == 0) { n /= 8; if (k++ == p) return 8; }
+  if (n % 4 == 0) { n /= 4; if (k++ == p) return 4; }
+  if (n % 2 == 0) { n /= 2; if (k++ == p) return 2; }
+  while (n % 3 == 0) { n /= 3; if (k++ == p) return 3; }
+  while (n % 5 == 0) { n /= 5; if (k++ == p) return 5; }
+  return 0;
+}
+
+// Lines are kept in shared memory with a stride of n + 1 complex values, and consecutive
+// threads take the same butterfly of consecutive lines: both keep the Stockham reads and
+// writes of a warp on distinct banks.
+__host__ __device__ constexpr int line_stride(int n) { return n + 1; }
+
+// One Stockham pass of radix R over `lines` sequences of length n (src -> dst).
+template <int R>
+__device__ __forceinline__ void fft_pass(const float2* __restrict__ src, float2* __restrict__ dst,
+                                         int lines, int n, int Ns, const float2* __restrict__ tw,
+                                         const FftPlan& pl) {
+  const int m = n / R;
+  const int step = n / (Ns * R);
+  const int ls = line_stride(n);
+  for (int t = threadIdx.x; t < lines * m; t += blockDim.x) {
+    const int j = t / lines;
+    const int line = t - j * lines;
+    const int k = j % Ns;
+    const float2* in = src + line * ls;
+    float2* o = dst + line * ls;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = in[j + r * m];
+#pragma unroll
+    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * step]);
+    if (R == 8) dft8(v);
+    else if (R == 4) dft4(v);
+    else if (R == 2) dft2(v);
+    else if (R == 3) dft_generic<R>(v, pl.root3);
+    else dft_generic<R>(v, pl.root5);
+    const int idx = (j / Ns) * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) o[idx + r * Ns] = v[r];
+  }
+}
+
+// Compile-time length: the pass sequence unrolled, every divisor a constant.
+template <int N, int P, int Ns>
+__device__ __forceinline__ void run_passes(float2*& src, float2*& dst,
+                                           const float2* __restrict__ tw, const FftPlan& pl) {
+  if constexpr (P < plan_np(N)) {
+    constexpr int R = plan_radix(N, P);
+    fft_pass<R>(src, dst, kLines, N, Ns, tw, pl);
+    __syncthreads();
+    float2* t2 = src;
+    src = dst;
+    dst = t2;
+    run_passes<N, P + 1, Ns * R>(src, dst, tw, pl);
+  }
+}
+
+// Inverse FFT (sign +1, unnormalised) of kLines sequences of length n stored with line
+// stride n + 1 in `a`; `b` is scratch of the same size.  Returns the buffer holding the
+// result.  NC = n at compile time, or 0.
+template <int NC>
+__device__ float2* fft_lines(float2* a, float2* b, const FftPlan& pl,
+                             const float2* __restrict__ tw) {
+  float2* src = a;
+  float2* dst = b;
+  if constexpr (NC != 0) {
+    run_passes<NC, 0, 1>(src, dst, tw, pl);
+  } else {
+    const int n = pl.n;
+    int Ns = 1;
+    for (int p = 0; p < pl.np; ++p) {
+      const int R = pl.radix[p];
+      switch (R) {
+        case 8: fft_pass<8>(src, dst, kLines, n, Ns, tw, pl); break;
+        case 4: fft_pass<4>(src, dst, kLines, n, Ns, tw, pl); break;
+        case 2: fft_pass<2>(src, dst, kLines, n, Ns, tw, pl); break;
+        case 3: fft_pass<3>(src, dst, kLines, n, Ns, tw, pl); break;
+        default: fft_pass<5>(src, dst, kLines, n, Ns, tw, pl); break;
+      }
+      __syncthreads();
+      float2* t2 = src;
+      src = dst;
+      dst = t2;
+      Ns *= R;
+    }
+  }
+  return src;
+}
+
+// Index of the i-th kept frequency of an axis: the `nk` frequencies |q| <= R around 0
+// (all n of them when 2R + 1 >= n).
+__device__ __forceinline__ int kept_index(int i, int nk, int R, int n) {
+  return nk == n ? i : (i - R + n) % n;
+}
+
+struct SynthArgs {
+  int N, H, R, nk, Cp, s0, ns;
+  const float2* spec;      // [a][b][c] slot spectrum
+  const uint16_t* table;   // [a][b][c] shell codes
+  float2* G;               // [s][x][bk][c]   (c < Cp)
+  float2* Hh;              // [s][x][y][c]
+  float* fields;           // [shell][N^3], shell index s0 + s
+  __nv_bfloat16* hi;       // optional [shell][N^3]
+  __nv_bfloat16* lo;
+  const float2* tw;        // [N] e^{+2 pi i k / N}
+};
+
+// X pass: block (bk, c-run).  Spectrum and table columns are read once for all shells.
+template <int NC>
+__global__ void __launch_bounds__(kThreads) synth_x_kernel(SynthArgs A, FftPlan pl) {
+  extern __shared__ float2 sm[];
+  const int N = NC ? NC : A.N, nk = A.nk;
+  const int ls = line_stride(N);
+  float2* buf0 = sm;                       // kLines lines
+  float2* buf1 = buf0 + kLines * ls;       // kLines lines
+  float2* tw = buf1 + kLines * ls;         // N
+  float2* sS = tw + N;                     // nk * kLines
+  uint16_t* sT = reinterpret_cast<uint16_t*>(sS + nk * kLines);  // nk * kLines
+  const int bk = blockIdx.x;
+  const int c0 = blockIdx.y * kLines;
+  const int b = kept_index(bk, nk, A.R, N);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = A.tw[i];
+  for (int i = threadIdx.x; i < nk * kLines; i += blockDim.x) {
+    const int ak = i / kLines, l = i - ak * kLines;
+    const int a = kept_index(ak, nk, A.R, N);
+    const int c = c0 + l;
+    float2 v = make_float2(0.f, 0.f);
+    uint16_t code = 0xFF;
+    if (c < A.H && c <= A.R) {
+      const int64_t m = ((int64_t)a * N + b) * A.H + c;
+      v = A.spec[m];
+      code = A.table[m];
+    }
+    sS[i] = v;
+    sT[i] = code;
+  }
+  __syncthreads();
+  for (int s = 0; s < A.ns; ++s) {
+    for (int i = threadIdx.x; i < kLines * N; i += blockDim.x) {
+      const int a = i / kLines, l = i - a * kLines;
+      // position a of line l holds frequency index a
+      const int qa = fft_freq(a, N);
+      float2 v = make_float2(0.f, 0.f);
+      if (nk == N || (qa >= -A.R && qa <= A.R)) {
+        const int ak = nk == N ? a : qa + A.R;
+        if (in_shell(sT[ak * kLines + l], A.s0 + s)) v = sS[ak * kLines + l];
+      }
+      buf0[l * ls + a] = v;
+    }
+    __syncthreads();
+    const float2* res = fft_lines<NC>(buf0, buf1, pl, tw);
+    // G[s][x][bk][c0 + l]
+    float2* g = A.G + (((int64_t)s * N) * nk + bk) * A.Cp + c0;
+    for (int i = threadIdx.x; i < kLines * N; i += blockDim.x) {
+      const int x = i / kLines, l = i - x * kLines;
+      g[(int64_t)x * nk * A.Cp + l] = res[l * ls + x];
+    }
+    __syncthreads();
+  }
+}
+
+// Y pass: block (x, c-run, shell).
+template <int NC>
+__global__ void __launch_bounds__(kThreads) synth_y_kernel(SynthArgs A, FftPlan pl) {
+  extern __shared__ float2 sm[];
+  const int N = NC ? NC : A.N, nk = A.nk;
+  const int ls = line_stride(N);
+  float2* buf0 = sm;
+  float2* buf1 = buf0 + kLines * ls;
+  float2* tw = buf1 + kLines * ls;
+  const int x = blockIdx.x;
+  const int c0 = blockIdx.y * kLines;
+  const int s = blockIdx.z;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = A.tw[i];
+  for (int i = threadIdx.x; i < kLines * ls; i += blockDim.x) buf0[i] = make_float2(0.f, 0.f);
+  __syncthreads();
+  const float2* g = A.G + (((int64_t)s * N + x) * nk) * A.Cp + c0;
+  for (int i = threadIdx.x; i < nk * kLines; i += blockDim.x) {
+    const int bk = i / kLines, l = i - bk * kLines;
+    const int b = kept_index(bk, nk, A.R, N);
+    buf0[l * ls + b] = g[(int64_t)bk * A.Cp + l];
+  }
+  __syncthreads();
+  const float2* res = fft_lines<NC>(buf0, buf1, pl, tw);
+  float2* h = A.Hh + (((int64_t)s * N + x) * N) * A.Cp + c0;
+  for (int i = threadIdx.x; i < kLines * N; i += blockDim.x) {
+    const int y = i / kLines, l = i - y * kLines;
+    h[(int64_t)y * A.Cp + l] = res[l * ls + y];
+  }
+}
+
+// Z pass: block (x, run of 2 kLines rows y, shell).  Line l packs rows y0 + 2l, y0 + 2l + 1.
+template <int NC>
+__global__ void __launch_bounds__(kThreads) synth_z_kernel(SynthArgs A, FftPlan pl) {
+  extern __shared__ float2 sm[];
+  const int N = NC ? NC : A.N;
+  const int ls = line_stride(N);
+  float2* buf0 = sm;
+  float2* buf1 = buf0 + kLines * ls;
+  float2* tw = buf1 + kLines * ls;
+  const int x = blockIdx.x;
+  const int y0 = blockIdx.y * 2 * kLines;
+  const int s = blockIdx.z;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = A.tw[i];
+  for (int i = threadIdx.x; i < kLines * ls; i += blockDim.x) buf0[i] = make_float2(0.f, 0.f);
+  __syncthreads();
+  const int cn = min(A.R, N / 2) + 1;  // q_c = 0 .. cn - 1 can be nonzero
+  const float2* h = A.Hh + (((int64_t)s * N + x) * N + y0) * A.Cp;
+  for (int i = threadIdx.x; i < kLines * cn; i += blockDim.x) {
+    const int l = i / cn, c = i - l * cn;
+    const int y1 = y0 + 2 * l;
+    if (y1 >= N) continue;
+    const float2 z1 = h[(int64_t)(2 * l) * A.Cp + c];
+    const float2 z2 = (y1 + 1 < N) ? h[(int64_t)(2 * l + 1) * A.Cp + c] : make_float2(0.f, 0.f);
+    float2* line = buf0 + l * ls;
+    if (c == 0 || 2 * c == N) {
+      line[c] = make_float2(z1.x, z2.x);
+    } else {
+      line[c] = make_float2(z1.x - z2.y, z1.y + z2.x);       // Z1 + i Z2
+      line[N - c] = make_float2(z1.x + z2.y, -z1.y + z2.x);  // conj(Z1) + i conj(Z2)
+    }
+  }
+  __syncthreads();
+  const float2* res = fft_lines<NC>(buf0, buf1, pl, tw);
+  const int64_t K = (int64_t)N * N * N;
+  const int64_t base = (int64_t)(A.s0 + s) * K + ((int64_t)x * N) * N;
+  float* f = A.fields + base;
+  for (int i = threadIdx.x; i < 2 * kLines * N; i += blockDim.x) {
+    const int r = i / N, z = i - r * N;  // output row y0 + r
+    const int y = y0 + r;
+    if (y >= N) continue;
+    const float2 w = res[(r >> 1) * ls + z];
+    const float v = (r & 1) ? w.y : w.x;
+    const int64_t o = (int64_t)y * N + z;
+    f[o] = v;
+    if (A.hi) {
+      const __nv_bfloat16 vh = __float2bfloat16_rn(v);
+      const __nv_bfloat16 vl = __float2bfloat16_rn(v - __bfloat162float(vh));
+      A.hi[base + o] = vh;
+      A.lo[base + o] = vl;
+    }
+  }
+}
+
+template <int NC>
+void run_synth(const SynthArgs& A, const FftPlan& pl, int nk, int Cp, int ns, size_t fft_smem,
+               size_t x_smem, cudaStream_t st) {
+  static bool attr_done[64] = {};
+  int dev = 0;
+  BSK_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && !attr_done[dev]) {
+    const int maxs = 227 * 1024;
+    BSK_CHECK_CUDA(cudaFuncSetAttribute(synth_x_kernel<NC>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, maxs));
+    BSK_CHECK_CUDA(cudaFuncSetAttribute(synth_y_kernel<NC>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, maxs));
+    BSK_CHECK_CUDA(cudaFuncSetAttribute(synth_z_kernel<NC>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, maxs));
+    attr_done[dev] = true;
+  }
+  const int N = A.N;
+  synth_x_kernel<NC><<<dim3(nk, Cp / kLines), kThreads, x_smem, st>>>(A, pl);
+  BSK_CHECK_CUDA(cudaGetLastError());
+  synth_y_kernel<NC><<<dim3(N, Cp / kLines, ns), kThreads, fft_smem, st>>>(A, pl);
+  BSK_CHECK_CUDA(cudaGetLastError());
+  synth_z_kernel<NC><<<dim3(N, (N + 2 * kLines - 1) / (2 * kLines), ns), kThreads, fft_smem, st>>>(
+      A, pl);
+  BSK_CHECK_CUDA(cudaGetLastError());
+}
+
+bool make_plan(int n, FftPlan& pl) {
+  pl.n = n;
+  pl.np = 0;
+  int m = n;
+  while (m % 8 == 0 && pl.np < 8) { pl.radix[pl.np++] = 8; m /= 8; }
+  if (m % 4 == 0 && pl.np < 8) { pl.radix[pl.np++] = 4; m /= 4; }
+  if (m % 2 == 0 && pl.np < 8) { pl.radix[pl.np++] = 2; m /= 2; }
+  while (m % 3 == 0 && pl.np < 8) { pl.radix[pl.np++] = 3; m /= 3; }
+  while (m % 5 == 0 && pl.np < 8) { pl.radix[pl.np++] = 5; m /= 5; }
+  for (int k = 0; k < 3; ++k)
+    pl.root3[k] = make_float2((float)std::cos(2 * M_PI * k / 3), (float)std::sin(2 * M_PI * k / 3));
+  for (int k = 0; k < 5; ++k)
+    pl.root5[k] = make_float2((float)std::cos(2 * M_PI * k / 5), (float)std::sin(2 * M_PI * k / 5));
+  return m == 1;
+}
+
+}  // namespace
+
+bool synth_supported(int n) {
+  FftPlan pl;
+  return n >= 8 && n <= 512 && n % 2 == 0 && make_plan(n, pl);
+}
+
+size_t synth_workspace_bytes(int n, int max_r, int batch) {
+  const int nk = std::min(2 * max_r + 1, n);
+  const int Cp = (max_r + 1 + kLines - 1) / kLines * kLines;
+  return ((size_t)batch * n * nk * Cp + (size_t)batch * n * n * Cp) * sizeof(float2) +
+         (size_t)n * sizeof(float2);
+}
+
+void synth_init_workspace(int N, void* work) {
+  std::vector<float2> htw(N);
+  for (int k = 0; k < N; ++k)
+    htw[k] = make_float2((float)std::cos(2 * M_PI * k / N), (float)std::sin(2 * M_PI * k / N));
+  BSK_CHECK_CUDA(cudaMemcpy(work, htw.data(), N * sizeof(float2), cudaMemcpyHostToDevice));
+}
+
+void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0, int ns, int R,
+                  void* work, float* fields, __nv_bfloat16* hi, __nv_bfloat16* lo,
+                  cudaStream_t st) {
+  FftPlan pl;
+  BSK_REQUIRE(make_plan(N, pl), BSK_ERR_UNSUPPORTED, "no FFT plan for this grid size");
+  R = std::min(R, N / 2);
+  const int nk = std::min(2 * R + 1, N);
+  const int Cp = (R + 1 + kLines - 1) / kLines * kLines;
+  SynthArgs A;
+  A.N = N;
+  A.H = N / 2 + 1;
+  A.R = R;
+  A.nk = nk;
+  A.Cp = Cp;
+  A.s0 = s0;
+  A.ns = ns;
+  A.spec = reinterpret_cast<const float2*>(spec);
+  A.table = table;
+  float2* tw = reinterpret_cast<float2*>(work);
+  A.G = tw + N;
+  A.Hh = A.G + (size_t)ns * N * nk * Cp;
+  A.fields = fields;
+  A.hi = hi;
+  A.lo = lo;
+  A.tw = tw;
+  const size_t fft_smem = (2 * (size_t)kLines * (N + 1) + N) * sizeof(float2);
+  const size_t x_smem = fft_smem + (size_t)nk * kLines * (sizeof(float2) + sizeof(uint16_t));
+  BSK_REQUIRE(x_smem <= 227 * 1024, BSK_ERR_UNSUPPORTED, "grid too large for the field synthesis");
+  switch (N) {
+    case 48: run_synth<48>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+    case 96: run_synth<96>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+    case 192: run_synth<192>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+    case 384: run_synth<384>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+    case 480: run_synth<480>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+    default: run_synth<0>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+  }
+}
+
+}  // namespace bsk
