@@ -316,38 +316,54 @@ __global__ void __launch_bounds__(kThreads) synth_z_kernel(SynthArgs A, FftPlan 
   __syncthreads();
   const int cn = min(A.R, N / 2) + 1;  // q_c = 0 .. cn - 1 can be nonzero
   const float2* h = A.Hh + (((int64_t)s * N + x) * N + y0) * A.Cp;
-  for (int i = threadIdx.x; i < kLines * cn; i += blockDim.x) {
-    const int l = i / cn, c = i - l * cn;
+  {
+    // 16 threads per line, q_c strided by 16
+    const int l = threadIdx.x >> 4;
     const int y1 = y0 + 2 * l;
-    if (y1 >= N) continue;
-    const float2 z1 = h[(int64_t)(2 * l) * A.Cp + c];
-    const float2 z2 = (y1 + 1 < N) ? h[(int64_t)(2 * l + 1) * A.Cp + c] : make_float2(0.f, 0.f);
     float2* line = buf0 + l * ls;
-    if (c == 0 || 2 * c == N) {
-      line[c] = make_float2(z1.x, z2.x);
-    } else {
-      line[c] = make_float2(z1.x - z2.y, z1.y + z2.x);       // Z1 + i Z2
-      line[N - c] = make_float2(z1.x + z2.y, -z1.y + z2.x);  // conj(Z1) + i conj(Z2)
+    if (y1 < N) {
+      for (int c = threadIdx.x & 15; c < cn; c += 16) {
+        const float2 z1 = h[(int64_t)(2 * l) * A.Cp + c];
+        const float2 z2 =
+            (y1 + 1 < N) ? h[(int64_t)(2 * l + 1) * A.Cp + c] : make_float2(0.f, 0.f);
+        if (c == 0 || 2 * c == N) {
+          line[c] = make_float2(z1.x, z2.x);
+        } else {
+          line[c] = make_float2(z1.x - z2.y, z1.y + z2.x);       // Z1 + i Z2
+          line[N - c] = make_float2(z1.x + z2.y, -z1.y + z2.x);  // conj(Z1) + i conj(Z2)
+        }
+      }
     }
   }
   __syncthreads();
   const float2* res = fft_lines<NC>(buf0, buf1, pl, tw);
   const int64_t K = (int64_t)N * N * N;
   const int64_t base = (int64_t)(A.s0 + s) * K + ((int64_t)x * N) * N;
-  float* f = A.fields + base;
-  for (int i = threadIdx.x; i < 2 * kLines * N; i += blockDim.x) {
-    const int r = i / N, z = i - r * N;  // output row y0 + r
+  // four consecutive z per thread: 16-byte field stores, 8-byte hi / lo stores (N % 4 == 0)
+  const int nq = N / 4;
+  for (int i = threadIdx.x; i < 2 * kLines * nq; i += blockDim.x) {
+    const int r = i / nq, z = (i - r * nq) * 4;  // output row y0 + r
     const int y = y0 + r;
     if (y >= N) continue;
-    const float2 w = res[(r >> 1) * ls + z];
-    const float v = (r & 1) ? w.y : w.x;
-    const int64_t o = (int64_t)y * N + z;
-    f[o] = v;
+    const float2* w = res + (r >> 1) * ls + z;
+    float4 v;
+    if (r & 1) v = make_float4(w[0].y, w[1].y, w[2].y, w[3].y);
+    else v = make_float4(w[0].x, w[1].x, w[2].x, w[3].x);
+    const int64_t o = base + (int64_t)y * N + z;
+    *reinterpret_cast<float4*>(A.fields + o) = v;
     if (A.hi) {
-      const __nv_bfloat16 vh = __float2bfloat16_rn(v);
-      const __nv_bfloat16 vl = __float2bfloat16_rn(v - __bfloat162float(vh));
-      A.hi[base + o] = vh;
-      A.lo[base + o] = vl;
+      const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y);
+      const __nv_bfloat162 h23 = __floats2bfloat162_rn(v.z, v.w);
+      const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
+      const __nv_bfloat162 l01 = __floats2bfloat162_rn(v.x - f01.x, v.y - f01.y);
+      const __nv_bfloat162 l23 = __floats2bfloat162_rn(v.z - f23.x, v.w - f23.y);
+      uint2 hv, lv;
+      hv.x = *reinterpret_cast<const uint32_t*>(&h01);
+      hv.y = *reinterpret_cast<const uint32_t*>(&h23);
+      lv.x = *reinterpret_cast<const uint32_t*>(&l01);
+      lv.y = *reinterpret_cast<const uint32_t*>(&l23);
+      *reinterpret_cast<uint2*>(A.hi + o) = hv;
+      *reinterpret_cast<uint2*>(A.lo + o) = lv;
     }
   }
 }
@@ -398,7 +414,7 @@ bool make_plan(int n, FftPlan& pl) {
 
 bool synth_supported(int n) {
   FftPlan pl;
-  return n >= 8 && n <= 512 && n % 2 == 0 && make_plan(n, pl);
+  return n >= 8 && n <= 512 && n % 4 == 0 && make_plan(n, pl);
 }
 
 size_t synth_workspace_bytes(int n, int max_r, int batch) {
