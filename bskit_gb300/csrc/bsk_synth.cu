@@ -72,6 +72,36 @@ __device__ __forceinline__ void dft8(float2* v) {
   v[3] = cadd(e[3], t3);
   v[7] = csub(e[3], t3);
 }
+__device__ __forceinline__ void dft16(float2* v) {
+  // 16 = 4 x 4: DFT4 over a of v[4a + b], twiddle e^{2 pi i b c / 16}, DFT4 over b
+  float2 y[4][4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    float2 t[4] = {v[b], v[4 + b], v[8 + b], v[12 + b]};
+    dft4(t);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) y[b][c] = t[c];
+  }
+  const float c1 = 0.92387953251128676f, s1 = 0.38268343236508977f;  // cos, sin(pi/8)
+  const float h = 0.70710678118654752f;
+  // e^{2 pi i k / 16} for k = b c: k = 1, 2, 3, 4, 6, 9
+  y[1][1] = cmul(y[1][1], make_float2(c1, s1));
+  y[1][2] = cmul(y[1][2], make_float2(h, h));
+  y[1][3] = cmul(y[1][3], make_float2(s1, c1));
+  y[2][1] = cmul(y[2][1], make_float2(h, h));
+  y[2][2] = mul_i(y[2][2]);
+  y[2][3] = cmul(y[2][3], make_float2(-h, h));
+  y[3][1] = cmul(y[3][1], make_float2(s1, c1));
+  y[3][2] = cmul(y[3][2], make_float2(-h, h));
+  y[3][3] = cmul(y[3][3], make_float2(-c1, -s1));
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float2 t[4] = {y[0][c], y[1][c], y[2][c], y[3][c]};
+    dft4(t);
+#pragma unroll
+    for (int d = 0; d < 4; ++d) v[c + 4 * d] = t[d];
+  }
+}
 template <int R>
 __device__ __forceinline__ void dft_generic(float2* v, const float2* roots) {
   float2 out[R];
@@ -89,15 +119,16 @@ __device__ __forceinline__ void dft_generic(float2* v, const float2* roots) {
 struct FftPlan {
   int n;
   int np;
-  int radix[8];
+  int radix[8];  // 16, 8, 4, 2, 3 or 5
   float2 root3[3];
   float2 root5[5];
 };
 
-// Radix plan of a length: 8s, then a 4 and a 2, then 3s and 5s (constexpr, so that a
+// Radix plan of a length: 16s, 8s, then a 4 and a 2, then 3s and 5s (constexpr, so that a
 // compile-time length gets a fully unrolled pass sequence).
 __host__ __device__ constexpr int plan_np(int n) {
   int np = 0;
+  while (n % 16 == 0) { n /= 16; ++np; }
   while (n % 8 == 0) { n /= 8; ++np; }
   if (n % 4 == 0) { n /= 4; ++np; }
   if (n % 2 == 0) { n /= 2; ++np; }
@@ -107,6 +138,7 @@ __host__ __device__ constexpr int plan_np(int n) {
 }
 __host__ __device__ constexpr int plan_radix(int n, int p) {
   int k = 0;
+  while (n % 16 == 0) { n /= 16; if (k++ == p) return 16; }
   while (n % 8 == 0) { n /= 8; if (k++ == p) return 8; }
   if (n % 4 == 0) { n /= 4; if (k++ == p) return 4; }
   if (n % 2 == 0) { n /= 2; if (k++ == p) return 2; }
@@ -137,9 +169,12 @@ __device__ __forceinline__ void fft_pass(const float2* __restrict__ src, float2*
     float2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = in[j + r * m];
+    if (Ns > 1) {  // the first pass has k = 0: unit twiddles
 #pragma unroll
-    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * step]);
-    if (R == 8) dft8(v);
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * step]);
+    }
+    if (R == 16) dft16(v);
+    else if (R == 8) dft8(v);
     else if (R == 4) dft4(v);
     else if (R == 2) dft2(v);
     else if (R == 3) dft_generic<R>(v, pl.root3);
@@ -181,6 +216,7 @@ __device__ float2* fft_lines(float2* a, float2* b, const FftPlan& pl,
     for (int p = 0; p < pl.np; ++p) {
       const int R = pl.radix[p];
       switch (R) {
+        case 16: fft_pass<16>(src, dst, kLines, n, Ns, tw, pl); break;
         case 8: fft_pass<8>(src, dst, kLines, n, Ns, tw, pl); break;
         case 4: fft_pass<4>(src, dst, kLines, n, Ns, tw, pl); break;
         case 2: fft_pass<2>(src, dst, kLines, n, Ns, tw, pl); break;
@@ -398,6 +434,7 @@ bool make_plan(int n, FftPlan& pl) {
   pl.n = n;
   pl.np = 0;
   int m = n;
+  while (m % 16 == 0 && pl.np < 8) { pl.radix[pl.np++] = 16; m /= 16; }
   while (m % 8 == 0 && pl.np < 8) { pl.radix[pl.np++] = 8; m /= 8; }
   if (m % 4 == 0 && pl.np < 8) { pl.radix[pl.np++] = 4; m /= 4; }
   if (m % 2 == 0 && pl.np < 8) { pl.radix[pl.np++] = 2; m /= 2; }
