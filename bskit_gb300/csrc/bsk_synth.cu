@@ -119,32 +119,63 @@ __device__ __forceinline__ void dft_generic(float2* v, const float2* roots) {
 struct FftPlan {
   int n;
   int np;
-  int radix[8];  // 16, 8, 4, 2, 3 or 5
+  int radix[8];  // 16, 24, 12, 8, 6, 4, 2, 3 or 5
   float2 root3[3];
   float2 root5[5];
+  float2 rootc[24];  // e^{+2 pi i k / Rc} of the plan's composite radix Rc (24, 12 or 6)
 };
 
-// Radix plan of a length: 16s, 8s, then a 4 and a 2, then 3s and 5s (constexpr, so that a
-// compile-time length gets a fully unrolled pass sequence).
-__host__ __device__ constexpr int plan_np(int n) {
-  int np = 0;
-  while (n % 16 == 0) { n /= 16; ++np; }
-  while (n % 8 == 0) { n /= 8; ++np; }
-  if (n % 4 == 0) { n /= 4; ++np; }
-  if (n % 2 == 0) { n /= 2; ++np; }
-  while (n % 3 == 0) { n /= 3; ++np; }
-  while (n % 5 == 0) { n /= 5; ++np; }
-  return n == 1 ? np : -1;
+template <int R>
+__device__ __forceinline__ void dft_small(float2* v, const FftPlan& pl) {
+  if (R == 8) dft8(v);
+  else if (R == 4) dft4(v);
+  else if (R == 2) dft2(v);
+  else if (R == 3) dft_generic<3>(v, pl.root3);
+  else dft_generic<5>(v, pl.root5);
 }
+
+// R = R1 R2 point DFT: input r = R2 a + b, output q = c + R1 d:
+// X[c + R1 d] = sum_b e^{2 pi i b d / R2} e^{2 pi i b c / R} sum_a v[R2 a + b] e^{2 pi i a c / R1}.
+template <int R1, int R2>
+__device__ __forceinline__ void dft_comp(float2* v, const FftPlan& pl) {
+  float2 y[R2][R1];
+#pragma unroll
+  for (int b = 0; b < R2; ++b) {
+    float2 t[R1];
+#pragma unroll
+    for (int a = 0; a < R1; ++a) t[a] = v[R2 * a + b];
+    dft_small<R1>(t, pl);
+#pragma unroll
+    for (int c = 0; c < R1; ++c) y[b][c] = b && c ? cmul(t[c], pl.rootc[b * c]) : t[c];
+  }
+#pragma unroll
+  for (int c = 0; c < R1; ++c) {
+    float2 t[R2];
+#pragma unroll
+    for (int b = 0; b < R2; ++b) t[b] = y[b][c];
+    dft_small<R2>(t, pl);
+#pragma unroll
+    for (int d = 0; d < R2; ++d) v[c + R1 * d] = t[d];
+  }
+}
+
+// Radix plan of a length: 16s, then one of 24 / 12 / 8 / 6 / 4 / 2, then 3s and 5s (constexpr, so that a
+// compile-time length gets a fully unrolled pass sequence).
+// The p-th radix of a length's plan (0 past the end, -1 when the length does not factor).
 __host__ __device__ constexpr int plan_radix(int n, int p) {
   int k = 0;
   while (n % 16 == 0) { n /= 16; if (k++ == p) return 16; }
-  while (n % 8 == 0) { n /= 8; if (k++ == p) return 8; }
-  if (n % 4 == 0) { n /= 4; if (k++ == p) return 4; }
-  if (n % 2 == 0) { n /= 2; if (k++ == p) return 2; }
+  const int comp[6] = {24, 12, 8, 6, 4, 2};  // at most one of these, 2^a 3 first
+  for (int c : comp)
+    if (n % c == 0) { n /= c; if (k++ == p) return c; break; }
   while (n % 3 == 0) { n /= 3; if (k++ == p) return 3; }
   while (n % 5 == 0) { n /= 5; if (k++ == p) return 5; }
-  return 0;
+  return n == 1 ? 0 : -1;
+}
+__host__ __device__ constexpr int plan_np(int n) {
+  int p = 0;
+  while (plan_radix(n, p) > 0) ++p;
+  return plan_radix(n, p) == 0 ? p : -1;
 }
 
 // Lines are kept in shared memory with a stride of n + 1 complex values, and consecutive
@@ -174,11 +205,10 @@ __device__ __forceinline__ void fft_pass(const float2* __restrict__ src, float2*
       for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * step]);
     }
     if (R == 16) dft16(v);
-    else if (R == 8) dft8(v);
-    else if (R == 4) dft4(v);
-    else if (R == 2) dft2(v);
-    else if (R == 3) dft_generic<R>(v, pl.root3);
-    else dft_generic<R>(v, pl.root5);
+    else if (R == 24) dft_comp<8, 3>(v, pl);
+    else if (R == 12) dft_comp<4, 3>(v, pl);
+    else if (R == 6) dft_comp<2, 3>(v, pl);
+    else dft_small<R>(v, pl);
     const int idx = (j / Ns) * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) o[idx + r * Ns] = v[r];
@@ -217,6 +247,9 @@ __device__ float2* fft_lines(float2* a, float2* b, const FftPlan& pl,
       const int R = pl.radix[p];
       switch (R) {
         case 16: fft_pass<16>(src, dst, kLines, n, Ns, tw, pl); break;
+        case 24: fft_pass<24>(src, dst, kLines, n, Ns, tw, pl); break;
+        case 12: fft_pass<12>(src, dst, kLines, n, Ns, tw, pl); break;
+        case 6: fft_pass<6>(src, dst, kLines, n, Ns, tw, pl); break;
         case 8: fft_pass<8>(src, dst, kLines, n, Ns, tw, pl); break;
         case 4: fft_pass<4>(src, dst, kLines, n, Ns, tw, pl); break;
         case 2: fft_pass<2>(src, dst, kLines, n, Ns, tw, pl); break;
@@ -432,19 +465,21 @@ void run_synth(const SynthArgs& A, const FftPlan& pl, int nk, int Cp, int ns, si
 
 bool make_plan(int n, FftPlan& pl) {
   pl.n = n;
-  pl.np = 0;
-  int m = n;
-  while (m % 16 == 0 && pl.np < 8) { pl.radix[pl.np++] = 16; m /= 16; }
-  while (m % 8 == 0 && pl.np < 8) { pl.radix[pl.np++] = 8; m /= 8; }
-  if (m % 4 == 0 && pl.np < 8) { pl.radix[pl.np++] = 4; m /= 4; }
-  if (m % 2 == 0 && pl.np < 8) { pl.radix[pl.np++] = 2; m /= 2; }
-  while (m % 3 == 0 && pl.np < 8) { pl.radix[pl.np++] = 3; m /= 3; }
-  while (m % 5 == 0 && pl.np < 8) { pl.radix[pl.np++] = 5; m /= 5; }
+  pl.np = plan_np(n);
+  if (pl.np <= 0 || pl.np > 8) return false;
+  int rc = 0;
+  for (int p = 0; p < pl.np; ++p) {
+    pl.radix[p] = plan_radix(n, p);
+    if (pl.radix[p] == 24 || pl.radix[p] == 12 || pl.radix[p] == 6) rc = pl.radix[p];
+  }
   for (int k = 0; k < 3; ++k)
     pl.root3[k] = make_float2((float)std::cos(2 * M_PI * k / 3), (float)std::sin(2 * M_PI * k / 3));
   for (int k = 0; k < 5; ++k)
     pl.root5[k] = make_float2((float)std::cos(2 * M_PI * k / 5), (float)std::sin(2 * M_PI * k / 5));
-  return m == 1;
+  for (int k = 0; k < 24; ++k)
+    pl.rootc[k] = rc ? make_float2((float)std::cos(2 * M_PI * k / rc), (float)std::sin(2 * M_PI * k / rc))
+                     : make_float2(1.f, 0.f);
+  return true;
 }
 
 }  // namespace

@@ -110,8 +110,11 @@ def test_gridinfo_exact_vs_oracle(cuda, grid):
     assert np.allclose(km[ok], kmo[ok], rtol=1e-12, atol=0)
 
 
-def test_fields_match_oracle_native(cuda):
-    n, box, edges, _ = _small(32, 100.0, 2)
+@pytest.mark.parametrize("n", [32, 40, 56])
+def test_fields_match_oracle_native(cuda, n):
+    # 32 and 40: the field synthesis (compile-time-free plans 16x2, 8x5); 56 = 8 x 7 has no
+    # synthesis plan and takes the filter + cuFFT C2R path
+    n, box, edges, _ = _small(n, 100.0, 2)
     delta = synthetic.lognormal_mesh(n, box, seed=11)
     plan = Plan(n, box, edges, grid="native")
     plan.paint(0, torch.from_numpy(delta))
