@@ -247,20 +247,54 @@ def run_ours(args):
     ms_step = ms / args.steps
     value = world * args.steps / (ms / 1e3)
 
-    # ---- end to end through the public API: pinned host mesh in, B to host each step
+    # ---- end to end through the public API: pinned host mesh in, B to host each step.
+    # The host->device copy of step k+1 runs on a copy stream while step k computes
+    # (double-buffered device meshes); every copy of a timed step is issued after the
+    # start event, and the stop event follows the last step's device->host read.
     host = delta.cpu().pin_memory()
-    dmesh = torch.empty_like(delta)
+    bufs = [torch.empty_like(delta), torch.empty_like(delta)]
     out_host = torch.empty(len(tri), dtype=torch.float64).pin_memory()
+    copy_stream = torch.cuda.Stream(device=dev)
+    loaded = [torch.cuda.Event(), torch.cuda.Event()]
+    free = [torch.cuda.Event(), torch.cuda.Event()]
 
-    def e2e_step():
-        dmesh.copy_(host, non_blocking=True)
-        plan.paint(0, dmesh)
-        b = plan.measure_b(ts, precision=prec)
-        out_host.copy_(plan.normalize(b, ntri), non_blocking=True)
-        return out_host
+    def prefetch(k):
+        i = k % 2
+        copy_stream.wait_event(free[i])  # the paint that last read this buffer is done
+        with torch.cuda.stream(copy_stream):
+            bufs[i].copy_(host, non_blocking=True)
+            loaded[i].record(copy_stream)
 
-    e2e_ms, _ = timed(e2e_step, args.steps, 1)
+    def run_e2e(n):
+        copy_stream.wait_stream(stream)
+        prefetch(0)
+        for k in range(n):
+            i = k % 2
+            stream.wait_event(loaded[i])
+            plan.paint(0, bufs[i])
+            free[i].record(stream)
+            if k + 1 < n:
+                prefetch(k + 1)
+            b = plan.measure_b(ts, precision=prec)
+            out_host.copy_(plan.normalize(b, ntri), non_blocking=True)
+
+    run_e2e(2)
+    plan.sync_check()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    run_e2e(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
     e2e_value = world * args.steps / (e2e_ms / 1e3)
+    host_check = out_host.clone()
 
     # ---- contraction alone (fields and split cached): the dominant kernel
     plan.paint(0, delta)
@@ -359,7 +393,11 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "bispectra/s",
                 "h2d_bytes_per_step": int(host.numel() * 4),
                 "d2h_bytes_per_step": int(out_host.numel() * 8),
-                "ms_per_step": e2e_ms / args.steps},
+                "ms_per_step": e2e_ms / args.steps,
+                "pipelining": "next step's H2D copy overlaps this step's compute (copy stream, "
+                              "two device buffers)",
+                "result_matches_device_step": bool(torch.allclose(
+                    host_check, bn.detach().cpu().double(), rtol=1e-9, atol=0))},
         "gpu_launches": kernel_launches_per_step(plan, prec) * args.steps,
         "roofline": {"kernel": "contract_tc_kernel (tcgen05 bf16x3)", "bound": "tensor",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
