@@ -326,6 +326,33 @@ const std::vector<StreamGroup>& stream_groups(const bsk_triset* set, int C) {
 // FFT batch); shells at or beyond n are zero.
 void chunk_fields(bsk_plan* p, int slot, int s0, int C, float* dst, cudaStream_t st) {
   const FieldSlot& f = p->slot[slot];
+  // the synthesis needs its workspace: use it when held already or when the budget has
+  // room for it, else the filter + cuFFT path (whose buffers the plan always holds)
+  const bool ws_fits = p->synth_ws || p->mem_budget == 0 ||
+                       footprint(p) + (int64_t)p->synth_ws_bytes <= (int64_t)p->mem_budget;
+  if (p->use_synth && ws_fits) {
+    if (!p->synth_ws) {
+      p->synth_ws = dmalloc(p->synth_ws_bytes);
+      synth_init_workspace(p->Ng, p->synth_ws);
+    }
+    for (int b = 0; b < C; b += p->chunk) {
+      const int first = s0 + b;
+      const int ns = std::max(0, std::min(p->chunk, p->n - first));
+      if (ns == 0) {
+        BSK_CHECK_CUDA(cudaMemsetAsync(dst + (size_t)b * p->K, 0,
+                                       (size_t)(C - b) * p->K * sizeof(float), st));
+        break;
+      }
+      int R = 0;
+      for (int k = first; k < first + ns; ++k) R = std::max(R, p->shell_r[k]);
+      launch_synth(p->Ng, f.spec, p->table, first, ns, R, p->synth_ws, dst, nullptr, nullptr,
+                   st, s0);
+      if (ns < p->chunk)
+        BSK_CHECK_CUDA(cudaMemsetAsync(dst + (size_t)(b + ns) * p->K, 0,
+                                       (size_t)(p->chunk - ns) * p->K * sizeof(float), st));
+    }
+    return;
+  }
   bind_work(p, p->c2r, st);
   for (int b = 0; b < C; b += p->chunk) {
     const int first = s0 + b;

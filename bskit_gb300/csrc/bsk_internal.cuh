@@ -189,13 +189,14 @@ void launch_window(int N, float scale, cufftComplex* spec, const float* axis_w, 
                    cudaStream_t st);
 // Field synthesis: fields (and optionally the hi / lo planes) of shells [s0, s0 + ns)
 // from the slot spectrum by three pruned FFT passes; R = largest |q_c| of those shells.
+// Shell s is written at fields[(s - out_s0) K].
 bool synth_supported(int n);
 size_t synth_workspace_bytes(int n, int max_r, int batch);
 // Twiddle table at the start of the workspace (synchronous; once, after allocation).
 void synth_init_workspace(int n, void* work);
 void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0, int ns, int R,
                   void* work, float* fields, __nv_bfloat16* hi, __nv_bfloat16* lo,
-                  cudaStream_t st);
+                  cudaStream_t st, int out_s0 = 0);
 // FP32 -> (bf16 hi, bf16 lo) split, n elements.
 void launch_split(const float* in, __nv_bfloat16* hi, __nv_bfloat16* lo, int64_t n,
                   cudaStream_t st);

@@ -274,6 +274,7 @@ __device__ __forceinline__ int kept_index(int i, int nk, int R, int n) {
 
 struct SynthArgs {
   int N, H, R, nk, Cp, s0, ns;
+  int out0;                // shell written at fields[0] (and hi/lo[0])
   const float2* spec;      // [a][b][c] slot spectrum
   const uint16_t* table;   // [a][b][c] shell codes
   float2* G;               // [s][x][bk][c]   (c < Cp)
@@ -407,7 +408,7 @@ __global__ void __launch_bounds__(kThreads) synth_z_kernel(SynthArgs A, FftPlan 
   __syncthreads();
   const float2* res = fft_lines<NC>(buf0, buf1, pl, tw);
   const int64_t K = (int64_t)N * N * N;
-  const int64_t base = (int64_t)(A.s0 + s) * K + ((int64_t)x * N) * N;
+  const int64_t base = (int64_t)(A.s0 + s - A.out0) * K + ((int64_t)x * N) * N;
   // four consecutive z per thread: 16-byte field stores, 8-byte hi / lo stores (N % 4 == 0)
   const int nq = N / 4;
   for (int i = threadIdx.x; i < 2 * kLines * nq; i += blockDim.x) {
@@ -505,7 +506,7 @@ void synth_init_workspace(int N, void* work) {
 
 void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0, int ns, int R,
                   void* work, float* fields, __nv_bfloat16* hi, __nv_bfloat16* lo,
-                  cudaStream_t st) {
+                  cudaStream_t st, int out_s0) {
   FftPlan pl;
   BSK_REQUIRE(make_plan(N, pl), BSK_ERR_UNSUPPORTED, "no FFT plan for this grid size");
   R = std::min(R, N / 2);
@@ -519,6 +520,7 @@ void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0
   A.Cp = Cp;
   A.s0 = s0;
   A.ns = ns;
+  A.out0 = out_s0;
   A.spec = reinterpret_cast<const float2*>(spec);
   A.table = table;
   float2* tw = reinterpret_cast<float2*>(work);

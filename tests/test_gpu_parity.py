@@ -305,8 +305,8 @@ def _streaming_case():
     return n, box, kw, B.generate_bin_edge_list(**kw)
 
 
-@pytest.mark.parametrize("prec", ["fp32", "bf16x3"])
-def test_shell_streaming_under_budget(cuda, prec):
+@pytest.mark.parametrize("prec,roomy", [("fp32", False), ("bf16x3", False), ("bf16x3", True)])
+def test_shell_streaming_under_budget(cuda, prec, roomy):
     n, box, kw, edges = _streaming_case()
     d1 = synthetic.lognormal_mesh(n, box, seed=31)
     d2 = synthetic.noisy_copy(d1, seed=32)
@@ -317,8 +317,12 @@ def test_shell_streaming_under_budget(cuda, prec):
     k = probe.ngrid ** 3
     probe.close()
     # room for one 8-shell chunk of three FP32 fields (+ the bf16 split), not for the
-    # 30 shells (32 with the FFT-batch padding) of one slot resident
+    # 30 shells (32 with the FFT-batch padding) of one slot resident; the tight budget
+    # leaves no room for the field-synthesis workspace (chunks come from the cuFFT path),
+    # the roomy one, just below the resident need, does
     room = 8 * k * (16 if prec == "bf16x3" else 12) + (1 << 20)
+    if roomy:
+        room = 32 * k * 8 - (4 << 20)
     plan = Plan(n, box, edges, mem_budget=base + room)
     plan.paint(0, torch.from_numpy(d1))
     plan.paint(1, torch.from_numpy(d2))
