@@ -309,6 +309,16 @@ def run_ours(args):
     peaks, peak_kind = measured_peaks()
     peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
     achieved = algo_flops / (c_ms / 1e3) / 1e12
+    # MMA work the kernel issues: per grid point, for every tile, 128 rows x (2 nc + nc)
+    # (bf16x3: hi x [Bhi; Blo] and lo x Bhi) multiply-adds
+    tiles, sum_nc, pair_rows = ts.schedule()
+    terms = 3 if prec == "bf16x3" else 1
+    issued_flops = 2.0 * 128 * terms * sum_nc * float(ng) ** 3
+    issued = {"flops_per_launch": issued_flops,
+              "tflops": issued_flops / (c_ms / 1e3) / 1e12,
+              "frac": issued_flops / (c_ms / 1e3) / 1e12 / peak,
+              "tiles": tiles, "sum_nc": sum_nc, "pair_rows": pair_rows,
+              "useful_fraction": len(tri) / (128.0 * sum_nc)}
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "contract_tc_traffic.json")) as f:
@@ -404,7 +414,8 @@ def run_ours(args):
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "%s bf16_tflops_sustained" % peak_kind,
                      "algorithmic_flops_per_launch": algo_flops,
-                     "launch_ms": c_ms},
+                     "launch_ms": c_ms,
+                     "issued": issued},
         "cpu_baseline": cpu,
         "clocks": clk,
         "cold": {"gridinfo_s": cold_gridinfo_s},

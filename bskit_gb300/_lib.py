@@ -49,6 +49,7 @@ SIGNATURES = [
     ("bsk_triset_size", _I64, [_VP]),
     ("bsk_paint", _INT, [_VP, _INT, _VP, _VP]),
     ("bsk_paint_cic", _INT, [_VP, _INT, _VP, _INT, _VP]),
+    ("bsk_triset_schedule", _INT, [_VP, _VP]),
     ("bsk_paint_subbox", _INT, [_VP, _INT, _VP, _INT, _INT, _INT, _INT, _VP]),
     ("bsk_compensate_cic", _INT, [_INT, _INT, _VP, _VP, _VP]),
     ("bsk_measure_b", _INT, [_VP, _VP, _INT, _INT, _INT, _INT, _VP, _VP]),

@@ -786,6 +786,20 @@ int bsk_triset_destroy(bsk_triset* set) {
 
 int64_t bsk_triset_size(const bsk_triset* set) { return set ? set->T : -1; }
 
+int bsk_triset_schedule(const bsk_triset* set, int64_t* out) {
+  return guarded([&] {
+    BSK_REQUIRE(set && out, BSK_ERR_ARG, "NULL argument");
+    int64_t cols = 0, rows = 0;
+    for (const TileDesc& d : set->sched.h_tiles) {
+      cols += d.nc;
+      rows += d.nrows;
+    }
+    out[0] = set->sched.n_tiles;
+    out[1] = cols;
+    out[2] = rows;
+  });
+}
+
 namespace bsk {
 namespace {
 // Factors 1/sqrt(1 - 2/3 sin^2(pi q / NmeshCIC)) for q = -N/2..N/2, the per-axis CIC

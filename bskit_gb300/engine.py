@@ -39,6 +39,12 @@ class TriangleSet:
         self.handle = h
         plan._sets.add(self)
 
+    def schedule(self):
+        """(tiles, sum of tile column counts, pair rows) of the contraction schedule."""
+        out = (ctypes.c_int64 * 3)()
+        _lib.call("bsk_triset_schedule", self.handle, out)
+        return int(out[0]), int(out[1]), int(out[2])
+
     def close(self):
         if getattr(self, "handle", None):
             with torch.cuda.device(self.plan.device):

@@ -118,6 +118,13 @@ int bsk_triset_create(bsk_plan* plan, int64_t n_tri, const int32_t* tri, bsk_tri
 int bsk_triset_destroy(bsk_triset* set);
 /* Number of triangles in a set. */
 int64_t bsk_triset_size(const bsk_triset* set);
+/*
+ * Contraction schedule of a set: out[0] = tiles (128 pair rows each), out[1] = sum of
+ * the tiles' column counts, out[2] = distinct (i, j) pair rows.  The tensor-core
+ * contraction issues 2 x 128 x 3 x out[1] flops per grid point for bf16x3 (useful:
+ * 2 x T).  Diagnostics; no counterpart in the reference.
+ */
+int bsk_triset_schedule(const bsk_triset* set, int64_t* out);
 
 /*
  * Forward-transform a real mesh into field slot `slot` (0, 1, 2 = the

@@ -271,6 +271,17 @@ def test_slab_ranges_sum_to_whole(cuda):
         assert np.abs(tot - whole).max() <= tol * np.abs(whole).max(), prec
 
 
+def test_schedule_covers_every_pair(cuda):
+    n, box, edges, tri = _small(64, 100.0, 2, 0.25)
+    plan = Plan(n, box, edges)
+    tiles, sum_nc, rows = plan.triangles(tri).schedule()
+    pairs = {(int(i), int(j)) for i, j, _ in tri}
+    assert rows == len(pairs)
+    assert tiles >= -(-rows // 128) and sum_nc % 16 == 0
+    assert len(tri) <= 128 * sum_nc
+    plan.close()
+
+
 def test_mem_budget_refuses_before_allocating(cuda):
     from bskit_gb300 import _lib
     n, box, edges, tri = _small(32, 100.0, 2)
