@@ -25,9 +25,10 @@
 //     add it into per-thread FP32 registers (round-to-nearest), and at the end
 //     of the slice add the entries that are triangle bins into the FP64 output
 //     (atomics).
-// The MMAs' completion is committed to two mbarriers per stage: one frees the
-// SMEM stage for the TMA producer, one frees the TMEM A stage for the A-operand
-// warps.  Stages are 128 points long because the single MMA-issuing thread,
+// The MMAs' completion is committed once per stage, to a ring of mbarriers that
+// the TMA producer (SMEM stage free), the A-operand warps (TMEM A stage free) and the
+// drain (accumulator ready) all wait on.  Stages are 128 points long because the
+// single MMA-issuing thread,
 // whose barrier waits and commits cost about as much as its MMAs, sets the pace:
 // longer stages spread that fixed cost over more tensor-core work.  Every
 // wait is bounded (globaltimer); on expiry the kernel records an error flag,
@@ -64,14 +65,20 @@ template <bool kTwoSrc> struct Ring {
 };
 constexpr int MAX_SSTAGES = 3;
 
+// One commit per stage serves every consumer of "the stage's MMAs are complete": the TMA
+// producer (SMEM stage free, SST stages later), the A-operand warps (TMEM A stage free,
+// ASTAGES later) and the drain (accumulator ready, the same stage).  DONE_RING > all of
+// those distances, so no barrier of the ring completes twice before each of its waiters
+// has seen the phase (each waiter's progress gates the MMA thread's).
+constexpr int DONE_RING = 4;
+static_assert(ACC_CHUNKS == 1, "the drain waits on the per-stage completion");
+
 struct Bars {
   uint64_t full[MAX_SSTAGES];      // TMA bytes landed
-  uint64_t released[MAX_SSTAGES];  // the MMAs reading the SMEM stage completed (tcgen05.commit)
+  uint64_t done[DONE_RING];        // the MMAs of stage c completed (tcgen05.commit), c % 4
   uint64_t afull[ASTAGES];         // A operand of the chunk is in TMEM (8 warp arrivals)
-  uint64_t aempty[ASTAGES];        // the MMAs reading the TMEM A stage completed
-  uint64_t accfull[NACC];
   uint64_t accempty[NACC];
-  uint64_t done;
+  uint64_t all_done;
   uint32_t tmem_base;
 };
 
@@ -315,17 +322,18 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < SST; ++s) {
       mbar_init(&bars->full[s], 1);
-      mbar_init(&bars->released[s], 1);
+
     }
     for (int a = 0; a < ASTAGES; ++a) {
       mbar_init(&bars->afull[a], 8);
-      mbar_init(&bars->aempty[a], 1);
+
     }
     for (int b = 0; b < NACC; ++b) {
-      mbar_init(&bars->accfull[b], 1);
+
       mbar_init(&bars->accempty[b], 8);
     }
-    mbar_init(&bars->done, 1);
+    for (int d = 0; d < DONE_RING; ++d) mbar_init(&bars->done[d], 1);
+    mbar_init(&bars->all_done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -359,8 +367,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                        4 * 128 * (box_rows(td.ni) + (one_src ? 0 : box_rows(td.nj))));
         for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
           const int s = chunk % SST;
-          const uint32_t ph = (chunk / SST) & 1;
-          if (!mbar_wait(&bars->released[s], ph ^ 1)) { ok = false; break; }
+          // SMEM stage s was last read by the MMAs of stage chunk - SST
+          if (chunk >= SST && !mbar_wait(&bars->done[(chunk - SST) % DONE_RING],
+                                          ((chunk - SST) / DONE_RING) & 1)) {
+            ok = false;
+            break;
+          }
           mbar_arrive_tx(&bars->full[s], bytes);
           const uint32_t st = sbase + s * STAGE_BYTES;
           const int xi = (int)x;
@@ -411,16 +423,13 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t kb_bytes = fused ? 2u * td.nc * 128u : (uint32_t)B_BLOCK;
         const uint32_t idesc_stack = idesc_bf16(terms >= 3 ? lo_row + td.nc : td.nc);
         const uint32_t idesc_hi = idesc_bf16(td.nc);
-        int in_grp = 0;
-        uint32_t d_tmem = 0, b = 0, accum = 0;
         for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
-          if (in_grp == 0) {
-            b = grp % NACC;
-            if (!mbar_wait(&bars->accempty[b], ((grp / NACC) & 1) ^ 1)) { ok = false; break; }
-            tc_fence_after();
-            d_tmem = tmem + ACC_COL + b * 128;
-            accum = 0;
-          }
+          // a fresh accumulator per stage, once the drain has emptied it
+          const uint32_t b = grp % NACC;
+          if (!mbar_wait(&bars->accempty[b], ((grp / NACC) & 1) ^ 1)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t d_tmem = tmem + ACC_COL + b * 128;
+          uint32_t accum = 0;
           const int s = chunk % SST;
           const uint32_t ph = (chunk / SST) & 1;
           const int a = chunk % ASTAGES;
@@ -438,18 +447,13 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (terms >= 3) mma_ts(d_tmem, a_lo + 8 * k, bdesc, idesc_hi, 1);
             accum = 1;
           }
-          tc_commit(&bars->released[s]);
-          tc_commit(&bars->aempty[a]);
-          if (++in_grp == ACC_CHUNKS || x + KCH >= x_end) {
-            tc_commit(&bars->accfull[b]);
-            ++grp;
-            in_grp = 0;
-          }
+          tc_commit(&bars->done[chunk % DONE_RING]);
+          ++grp;
         }
       }
       // all MMAs of this CTA complete before TMEM is released
-      tc_commit(&bars->done);
-      mbar_wait(&bars->done, 0);
+      tc_commit(&bars->all_done);
+      mbar_wait(&bars->all_done, 0);
     }
   } else if (warp < 10) {
     // ------------------------------------------------------------ accumulator drain
@@ -471,7 +475,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int c = 0; c < 32; ++c) acc[c] = 0.f;
       for (int64_t g = 0; g < ngrp; ++g, ++grp) {
         const uint32_t b = grp % NACC;
-        if (!__all_sync(0xffffffffu, mbar_wait(&bars->accfull[b], (grp / NACC) & 1))) {
+        if (!__all_sync(0xffffffffu,
+                        mbar_wait(&bars->done[grp % DONE_RING], (grp / DONE_RING) & 1))) {
           ok = false;
           break;
         }
@@ -531,9 +536,14 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int s = chunk % SST;
         const uint32_t ph = (chunk / SST) & 1;
         const int a = chunk % ASTAGES;
-        const uint32_t pa = (chunk / ASTAGES) & 1;
         if (!__all_sync(0xffffffffu, mbar_wait(&bars->full[s], ph))) { ok = false; break; }
-        if (!__all_sync(0xffffffffu, mbar_wait(&bars->aempty[a], pa ^ 1))) { ok = false; break; }
+        // TMEM A stage a was last read by the MMAs of stage chunk - ASTAGES
+        if (chunk >= ASTAGES &&
+            !__all_sync(0xffffffffu, mbar_wait(&bars->done[(chunk - ASTAGES) % DONE_RING],
+                                               ((chunk - ASTAGES) / DONE_RING) & 1))) {
+          ok = false;
+          break;
+        }
         tc_fence_after();
         const uint8_t* st = smem + s * STAGE_BYTES;
         const uint32_t a_hi = tmem + tlane + A_COL + a * 128 + half * 32;
