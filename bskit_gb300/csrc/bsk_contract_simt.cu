@@ -6,7 +6,8 @@
 // (double buffered, register prefetch of the next chunk), then a 4x4
 // register-tiled outer-product loop accumulates C[r][c] += P[r][x] * F3[c][x].
 // At the end of the slice the tile sums are added to the FP64 output with
-// atomics (only entries that are triangle bins).  Items are ordered slice-major
+// atomics (only entries that are triangle bins); warps whose 16 x 32 entries hold
+// no bin skip the multiply-adds.  Items are ordered slice-major
 // so that blocks running at the same time share field data in L2.
 #include "bsk_internal.cuh"
 
@@ -63,6 +64,17 @@ __global__ void __launch_bounds__(THREADS) contract_simt_kernel(
     for (int a = 0; a < 4; ++a)
 #pragma unroll
       for (int b = 0; b < 4; ++b) acc[a][b] = (Tacc)0;
+    // A warp (16 rows x 32 columns) whose entries hold no triangle bin skips the
+    // multiply-adds; it still loads its share of the tiles the whole block uses.
+    bool mine = false;
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int c = c0 + tx * 4 + q;
+        if (c < td.nc && map[td.map_off + c * ROWS + ty * 4 + p] >= 0) mine = true;
+      }
+    const bool warp_busy = __any_sync(0xffffffffu, mine);
 
     Tacc ra[16], rc[4];
     auto load = [&](int64_t x0) {
@@ -94,7 +106,7 @@ __global__ void __launch_bounds__(THREADS) contract_simt_kernel(
       const bool more = x0 + KC < x_end;
       if (more) load(x0 + KC);
 #pragma unroll 8
-      for (int k = 0; k < KC; ++k) {
+      for (int k = 0; k < KC && warp_busy; ++k) {
         Tacc a[4], b[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
