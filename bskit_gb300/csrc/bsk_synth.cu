@@ -20,7 +20,8 @@
 namespace bsk {
 namespace {
 
-constexpr int kLines = 16;  // lines (one 16-wide q_c run) per block
+constexpr int kLines = 16;   // lines (one 16-wide q_c run) per block of the X and Y passes
+constexpr int kZLines = 16;  // lines (two output rows each) per block of the Z pass
 constexpr int kThreads = 256;
 
 __device__ __forceinline__ int fft_freq(int a, int n) { return a < (n + 1) / 2 ? a : a - n; }
@@ -216,45 +217,45 @@ __device__ __forceinline__ void fft_pass(const float2* __restrict__ src, float2*
 }
 
 // Compile-time length: the pass sequence unrolled, every divisor a constant.
-template <int N, int P, int Ns>
+template <int N, int L, int P, int Ns>
 __device__ __forceinline__ void run_passes(float2*& src, float2*& dst,
                                            const float2* __restrict__ tw, const FftPlan& pl) {
   if constexpr (P < plan_np(N)) {
     constexpr int R = plan_radix(N, P);
-    fft_pass<R>(src, dst, kLines, N, Ns, tw, pl);
+    fft_pass<R>(src, dst, L, N, Ns, tw, pl);
     __syncthreads();
     float2* t2 = src;
     src = dst;
     dst = t2;
-    run_passes<N, P + 1, Ns * R>(src, dst, tw, pl);
+    run_passes<N, L, P + 1, Ns * R>(src, dst, tw, pl);
   }
 }
 
-// Inverse FFT (sign +1, unnormalised) of kLines sequences of length n stored with line
+// Inverse FFT (sign +1, unnormalised) of L sequences of length n stored with line
 // stride n + 1 in `a`; `b` is scratch of the same size.  Returns the buffer holding the
 // result.  NC = n at compile time, or 0.
-template <int NC>
+template <int NC, int L>
 __device__ float2* fft_lines(float2* a, float2* b, const FftPlan& pl,
                              const float2* __restrict__ tw) {
   float2* src = a;
   float2* dst = b;
   if constexpr (NC != 0) {
-    run_passes<NC, 0, 1>(src, dst, tw, pl);
+    run_passes<NC, L, 0, 1>(src, dst, tw, pl);
   } else {
     const int n = pl.n;
     int Ns = 1;
     for (int p = 0; p < pl.np; ++p) {
       const int R = pl.radix[p];
       switch (R) {
-        case 16: fft_pass<16>(src, dst, kLines, n, Ns, tw, pl); break;
-        case 24: fft_pass<24>(src, dst, kLines, n, Ns, tw, pl); break;
-        case 12: fft_pass<12>(src, dst, kLines, n, Ns, tw, pl); break;
-        case 6: fft_pass<6>(src, dst, kLines, n, Ns, tw, pl); break;
-        case 8: fft_pass<8>(src, dst, kLines, n, Ns, tw, pl); break;
-        case 4: fft_pass<4>(src, dst, kLines, n, Ns, tw, pl); break;
-        case 2: fft_pass<2>(src, dst, kLines, n, Ns, tw, pl); break;
-        case 3: fft_pass<3>(src, dst, kLines, n, Ns, tw, pl); break;
-        default: fft_pass<5>(src, dst, kLines, n, Ns, tw, pl); break;
+        case 16: fft_pass<16>(src, dst, L, n, Ns, tw, pl); break;
+        case 24: fft_pass<24>(src, dst, L, n, Ns, tw, pl); break;
+        case 12: fft_pass<12>(src, dst, L, n, Ns, tw, pl); break;
+        case 6: fft_pass<6>(src, dst, L, n, Ns, tw, pl); break;
+        case 8: fft_pass<8>(src, dst, L, n, Ns, tw, pl); break;
+        case 4: fft_pass<4>(src, dst, L, n, Ns, tw, pl); break;
+        case 2: fft_pass<2>(src, dst, L, n, Ns, tw, pl); break;
+        case 3: fft_pass<3>(src, dst, L, n, Ns, tw, pl); break;
+        default: fft_pass<5>(src, dst, L, n, Ns, tw, pl); break;
       }
       __syncthreads();
       float2* t2 = src;
@@ -328,7 +329,7 @@ __global__ void __launch_bounds__(kThreads) synth_x_kernel(SynthArgs A, FftPlan 
       buf0[l * ls + a] = v;
     }
     __syncthreads();
-    const float2* res = fft_lines<NC>(buf0, buf1, pl, tw);
+    const float2* res = fft_lines<NC, kLines>(buf0, buf1, pl, tw);
     // G[s][x][bk][c0 + l]
     float2* g = A.G + (((int64_t)s * N) * nk + bk) * A.Cp + c0;
     for (int i = threadIdx.x; i < kLines * N; i += blockDim.x) {
@@ -361,7 +362,7 @@ __global__ void __launch_bounds__(kThreads) synth_y_kernel(SynthArgs A, FftPlan 
     buf0[l * ls + b] = g[(int64_t)bk * A.Cp + l];
   }
   __syncthreads();
-  const float2* res = fft_lines<NC>(buf0, buf1, pl, tw);
+  const float2* res = fft_lines<NC, kLines>(buf0, buf1, pl, tw);
   float2* h = A.Hh + (((int64_t)s * N + x) * N) * A.Cp + c0;
   for (int i = threadIdx.x; i < kLines * N; i += blockDim.x) {
     const int y = i / kLines, l = i - y * kLines;
@@ -369,30 +370,31 @@ __global__ void __launch_bounds__(kThreads) synth_y_kernel(SynthArgs A, FftPlan 
   }
 }
 
-// Z pass: block (x, run of 2 kLines rows y, shell).  Line l packs rows y0 + 2l, y0 + 2l + 1.
+// Z pass: block (x, run of 2 kZLines rows y, shell).  Line l packs rows y0 + 2l, y0 + 2l + 1.
 template <int NC>
 __global__ void __launch_bounds__(kThreads) synth_z_kernel(SynthArgs A, FftPlan pl) {
   extern __shared__ float2 sm[];
   const int N = NC ? NC : A.N;
   const int ls = line_stride(N);
   float2* buf0 = sm;
-  float2* buf1 = buf0 + kLines * ls;
-  float2* tw = buf1 + kLines * ls;
+  float2* buf1 = buf0 + kZLines * ls;
+  float2* tw = buf1 + kZLines * ls;
   const int x = blockIdx.x;
-  const int y0 = blockIdx.y * 2 * kLines;
+  const int y0 = blockIdx.y * 2 * kZLines;
   const int s = blockIdx.z;
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = A.tw[i];
-  for (int i = threadIdx.x; i < kLines * ls; i += blockDim.x) buf0[i] = make_float2(0.f, 0.f);
+  for (int i = threadIdx.x; i < kZLines * ls; i += blockDim.x) buf0[i] = make_float2(0.f, 0.f);
   __syncthreads();
   const int cn = min(A.R, N / 2) + 1;  // q_c = 0 .. cn - 1 can be nonzero
   const float2* h = A.Hh + (((int64_t)s * N + x) * N + y0) * A.Cp;
   {
-    // 16 threads per line, q_c strided by 16
-    const int l = threadIdx.x >> 4;
+    // kThreads / kZLines threads per line, q_c strided by that
+    constexpr int tpl = kThreads / kZLines;
+    const int l = threadIdx.x / tpl;
     const int y1 = y0 + 2 * l;
     float2* line = buf0 + l * ls;
     if (y1 < N) {
-      for (int c = threadIdx.x & 15; c < cn; c += 16) {
+      for (int c = threadIdx.x % tpl; c < cn; c += tpl) {
         const float2 z1 = h[(int64_t)(2 * l) * A.Cp + c];
         const float2 z2 =
             (y1 + 1 < N) ? h[(int64_t)(2 * l + 1) * A.Cp + c] : make_float2(0.f, 0.f);
@@ -406,12 +408,12 @@ __global__ void __launch_bounds__(kThreads) synth_z_kernel(SynthArgs A, FftPlan 
     }
   }
   __syncthreads();
-  const float2* res = fft_lines<NC>(buf0, buf1, pl, tw);
+  const float2* res = fft_lines<NC, kZLines>(buf0, buf1, pl, tw);
   const int64_t K = (int64_t)N * N * N;
   const int64_t base = (int64_t)(A.s0 + s - A.out0) * K + ((int64_t)x * N) * N;
   // four consecutive z per thread: 16-byte field stores, 8-byte hi / lo stores (N % 4 == 0)
   const int nq = N / 4;
-  for (int i = threadIdx.x; i < 2 * kLines * nq; i += blockDim.x) {
+  for (int i = threadIdx.x; i < 2 * kZLines * nq; i += blockDim.x) {
     const int r = i / nq, z = (i - r * nq) * 4;  // output row y0 + r
     const int y = y0 + r;
     if (y >= N) continue;
@@ -459,7 +461,8 @@ void run_synth(const SynthArgs& A, const FftPlan& pl, int nk, int Cp, int ns, si
   BSK_CHECK_CUDA(cudaGetLastError());
   synth_y_kernel<NC><<<dim3(N, Cp / kLines, ns), kThreads, fft_smem, st>>>(A, pl);
   BSK_CHECK_CUDA(cudaGetLastError());
-  synth_z_kernel<NC><<<dim3(N, (N + 2 * kLines - 1) / (2 * kLines), ns), kThreads, fft_smem, st>>>(
+  const size_t z_smem = (2 * (size_t)kZLines * (N + 1) + N) * sizeof(float2);
+  synth_z_kernel<NC><<<dim3(N, (N + 2 * kZLines - 1) / (2 * kZLines), ns), kThreads, z_smem, st>>>(
       A, pl);
   BSK_CHECK_CUDA(cudaGetLastError());
 }
