@@ -48,7 +48,8 @@ def _abs_sums(fa, fb, fc, tri, box, n):
 def _check_b(b, bo, babs, prec):
     err = np.abs(b - bo)
     nrm = err / babs
-    rel = err / np.abs(bo)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rel = err / np.abs(bo)  # inf / nan on bins with no closed triangle
     well = np.abs(bo) >= 0.1 * babs
     print("%s: max nrm %.3g, max rel(well-conditioned, %d/%d bins) %.3g, median rel %.3g" %
           (prec, nrm.max(), well.sum(), len(bo), rel[well].max() if well.any() else 0,
