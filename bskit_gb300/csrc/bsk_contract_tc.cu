@@ -15,11 +15,12 @@
 //     row's F1_i, F2_j from SMEM, form P = F1_i*F2_j with packed f32x2
 //     arithmetic, split P = hi + lo (bf16 round-to-nearest) and store them with
 //     tcgen05.st into the 2-stage TMEM A-operand ring (lane = GEMM row);
-//   * warp 1 (one lane) issues, per 16-point K step, tcgen05.mma kind::f16 with
-//     A from TMEM and B from SMEM: hi x [Bhi; Blo] (N = 64 + nc: one MMA yields
-//     both hi*Bhi and hi*Blo) and, for bf16x3, lo x Bhi (N = nc).  The tensor
-//     core's FP32 accumulate truncates, so an accumulator is only ever fed one
-//     stage (16 MMAs) before it is handed over;
+//   * warp 1 runs the stage loop and one elected lane issues, per 16-point K step,
+//     tcgen05.mma kind::f16 with A from TMEM and B from SMEM: hi x [Bhi; Blo]
+//     (N = 2 nc, or 64 + nc with 2D copies: one MMA yields both hi*Bhi and hi*Blo)
+//     and, for bf16x3, lo x Bhi (N = nc).  The tensor core's FP32 accumulate
+//     truncates, so an accumulator is only ever fed one stage (16 MMAs) before it is
+//     handed over;
 //   * warps 2..9 (2 per lane quadrant, 32 columns each) drain each finished
 //     accumulator with tcgen05.ld (hi*B + lo*Bhi columns and hi*Blo columns),
 //     add it into per-thread FP32 registers (round-to-nearest), and at the end
@@ -27,12 +28,10 @@
 //     (atomics).
 // The MMAs' completion is committed once per stage, to a ring of mbarriers that
 // the TMA producer (SMEM stage free), the A-operand warps (TMEM A stage free) and the
-// drain (accumulator ready) all wait on.  Stages are 128 points long because the
-// single MMA-issuing thread,
-// whose barrier waits and commits cost about as much as its MMAs, sets the pace:
-// longer stages spread that fixed cost over more tensor-core work.  Every
-// wait is bounded (globaltimer); on expiry the kernel records an error flag,
-// stops issuing work, drains its own MMAs and frees TMEM.
+// drain (accumulator ready) all wait on.  Stages are 128 points long so that the fixed
+// cost of a stage's barrier round trips is spread over 16 MMAs.  Every wait is bounded
+// (globaltimer); on expiry the kernel records an error flag, stops issuing work, drains
+// its own MMAs and frees TMEM.
 #include <cuda.h>
 
 #include "bsk_internal.cuh"
@@ -196,6 +195,16 @@ __device__ __forceinline__ const CUtensorMap* by_rows(int n, const CUtensorMap* 
                                                       const CUtensorMap* m48,
                                                       const CUtensorMap* m64) {
   return n > 48 ? m64 : n > 32 ? m48 : n > 16 ? m32 : m16;
+}
+// One lane of a fully active warp (elect.sync picks the lowest active lane).
+__device__ __forceinline__ bool elect_one() {
+  uint32_t pred = 0;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "elect.sync _|p, 0xffffffff;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(pred));
+  return pred != 0;
 }
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -408,38 +417,43 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
-    if (lane == 0) {
-      uint32_t chunk = 0, grp = 0;
-      bool ok = true;
-      for (int64_t item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
-        const int64_t sl = item / n_tiles;
-        const TileDesc td = tiles[item % n_tiles];
-        const int64_t x_begin = k_begin + sl * SLICE;
-        const int64_t x_end = min(k_end, x_begin + SLICE);
-        // hi x [Bhi; Blo] (with 2D copies rows nc..63 of the hi block are not loaded:
-        // their accumulator columns are never read), lo x Bhi
-        // the lo rows of B sit right after the nc hi rows (one-copy loads) or 64 rows after
-        const int lo_row = fused ? td.nc : 64;
-        const uint32_t kb_bytes = fused ? 2u * td.nc * 128u : (uint32_t)B_BLOCK;
-        const uint32_t idesc_stack = idesc_bf16(terms >= 3 ? lo_row + td.nc : td.nc);
-        const uint32_t idesc_hi = idesc_bf16(td.nc);
-        for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
-          // a fresh accumulator per stage, once the drain has emptied it
-          const uint32_t b = grp % NACC;
-          if (!mbar_wait(&bars->accempty[b], ((grp / NACC) & 1) ^ 1)) { ok = false; break; }
-          tc_fence_after();
-          const uint32_t d_tmem = tmem + ACC_COL + b * 128;
+    // The whole warp runs the loop (barrier waits, stage addresses and descriptors are
+    // warp-uniform values) and one elected lane issues each stage's 16 MMAs and its commit
+    // as one straight run; a loop run by a single lane issued 3-4x slower.
+    uint32_t chunk = 0, grp = 0;
+    bool ok = true;
+    for (int64_t item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
+      const int64_t sl = item / n_tiles;
+      const TileDesc td = tiles[item % n_tiles];
+      const int64_t x_begin = k_begin + sl * SLICE;
+      const int64_t x_end = min(k_end, x_begin + SLICE);
+      // hi x [Bhi; Blo] (with 2D copies rows nc..63 of the hi block are not loaded:
+      // their accumulator columns are never read), lo x Bhi
+      // the lo rows of B sit right after the nc hi rows (one-copy loads) or 64 rows after
+      const int lo_row = fused ? td.nc : 64;
+      const uint32_t kb_bytes = fused ? 2u * td.nc * 128u : (uint32_t)B_BLOCK;
+      const uint32_t idesc_stack = idesc_bf16(terms >= 3 ? lo_row + td.nc : td.nc);
+      const uint32_t idesc_hi = idesc_bf16(td.nc);
+      for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
+        // a fresh accumulator per stage, once the drain has emptied it
+        const uint32_t b = grp % NACC;
+        const int s = chunk % SST;
+        const uint32_t ph = (chunk / SST) & 1;
+        const int a = chunk % ASTAGES;
+        const uint32_t pa = (chunk / ASTAGES) & 1;
+        if (!__all_sync(0xffffffffu, mbar_wait(&bars->accempty[b], ((grp / NACC) & 1) ^ 1) &&
+                                         mbar_wait(&bars->full[s], ph) &&
+                                         mbar_wait(&bars->afull[a], pa))) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d_tmem = tmem + ACC_COL + b * 128;
+        const uint32_t st = sbase + s * STAGE_BYTES;
+        const uint32_t a_hi = tmem + A_COL + a * 128;
+        const uint32_t a_lo = a_hi + 64;
+        if (elect_one()) {
           uint32_t accum = 0;
-          const int s = chunk % SST;
-          const uint32_t ph = (chunk / SST) & 1;
-          const int a = chunk % ASTAGES;
-          const uint32_t pa = (chunk / ASTAGES) & 1;
-          if (!mbar_wait(&bars->full[s], ph)) { ok = false; break; }
-          if (!mbar_wait(&bars->afull[a], pa)) { ok = false; break; }
-          tc_fence_after();
-          const uint32_t st = sbase + s * STAGE_BYTES;
-          const uint32_t a_hi = tmem + A_COL + a * 128;
-          const uint32_t a_lo = a_hi + 64;
 #pragma unroll
           for (int k = 0; k < KCH / 16; ++k) {
             const uint64_t bdesc = desc_sw128(st + (k >> 2) * kb_bytes + 32 * (k & 3));
@@ -448,13 +462,16 @@ __global__ void __launch_bounds__(THREADS, 1)
             accum = 1;
           }
           tc_commit(&bars->done[chunk % DONE_RING]);
-          ++grp;
         }
+        __syncwarp();
+        ++grp;
       }
-      // all MMAs of this CTA complete before TMEM is released
-      tc_commit(&bars->all_done);
-      mbar_wait(&bars->all_done, 0);
     }
+    // all MMAs of this CTA complete before TMEM is released (the elected lane is the
+    // same lane every time: elect.sync over a full warp picks its lowest lane)
+    if (elect_one()) tc_commit(&bars->all_done);
+    __syncwarp();
+    mbar_wait(&bars->all_done, 0);
   } else if (warp < 10) {
     // ------------------------------------------------------------ accumulator drain
     const int qd = warp & 3;
