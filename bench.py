@@ -42,6 +42,12 @@ WORKLOADS = {
                      "1024^3 all-triangle auto bispectrum: L=2000 Mpc/h, 38 shells dk=4kf from "
                      "kf to 0.3 kNyq, 5833 bins, lognormal float32 mesh (seed 1+rank), grid "
                      "info cached"),
+    # the headline's 384-point contraction grid with 15 shells (k from 7 kf in steps of 8 kf):
+    # a small case of the same field-synthesis kernels for multi-pass profiler captures
+    "mesh512_dk8": (512, 1000.0, 128.0, 8,
+                    "512^3 all-triangle auto bispectrum: L=1000 Mpc/h, 15 shells dk=8kf from 7kf "
+                    "to kNyq/2, 477 bins, lognormal float32 mesh (seed 1+rank), grid info cached",
+                    7.0),
 }
 NMESH, BOX = 512, 1000.0
 WORKLOAD = WORKLOADS["mesh512_all"][4]
@@ -80,14 +86,15 @@ def parse():
 
 def select_workload(name):
     global NMESH, BOX, WORKLOAD
-    NMESH, BOX, _, _, WORKLOAD = WORKLOADS[name]
+    NMESH, BOX, WORKLOAD = WORKLOADS[name][0], WORKLOADS[name][1], WORKLOADS[name][4]
 
 
 def workload_bins(name="mesh512_all"):
     from bskit_gb300 import bins
-    n, box, kmax, dk, _ = WORKLOADS[name]
+    n, box, kmax, dk = WORKLOADS[name][:4]
+    kmin = WORKLOADS[name][5] if len(WORKLOADS[name]) > 5 else 1.0
     kf = 2 * math.pi / box
-    kw = dict(kmin=kf, kmax=kmax * kf, dk=dk * kf)
+    kw = dict(kmin=kmin * kf, kmax=kmax * kf, dk=dk * kf)
     return bins.generate_bin_edge_list(**kw), bins.generate_triangle_bin_list(return_indices=True,
                                                                               **kw)
 
