@@ -340,103 +340,165 @@ __global__ void __launch_bounds__(kThreads) synth_x_kernel(SynthArgs A, FftPlan 
   }
 }
 
-// Y pass: block (x, c-run, shell).
+// The Y and Z passes are persistent: a block walks units (u, u + gridDim.x, ...) and,
+// while the FFT of one unit runs, the global loads of its share of the next unit's input
+// are already in flight into registers (kYPf / kZPf values per thread; inputs beyond
+// that, only possible for the largest shells, are read when the unit starts).
+constexpr int kYPf = 16;  // Y pass: kYPf * kThreads / kLines kept q_b per line
+constexpr int kZPf = 8;   // Z pass: kZPf * kThreads / kZLines nonzero q_c per line
+
+// Y pass: unit (x, c-run, shell).
 template <int NC>
-__global__ void __launch_bounds__(kThreads) synth_y_kernel(SynthArgs A, FftPlan pl) {
+__global__ void __launch_bounds__(kThreads, 2) synth_y_kernel(SynthArgs A, FftPlan pl, int units) {
   extern __shared__ float2 sm[];
   const int N = NC ? NC : A.N, nk = A.nk;
   const int ls = line_stride(N);
   float2* buf0 = sm;
   float2* buf1 = buf0 + kLines * ls;
   float2* tw = buf1 + kLines * ls;
-  const int x = blockIdx.x;
-  const int c0 = blockIdx.y * kLines;
-  const int s = blockIdx.z;
+  const int nrun = A.Cp / kLines;
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = A.tw[i];
-  for (int i = threadIdx.x; i < kLines * ls; i += blockDim.x) buf0[i] = make_float2(0.f, 0.f);
-  __syncthreads();
-  const float2* g = A.G + (((int64_t)s * N + x) * nk) * A.Cp + c0;
-  for (int i = threadIdx.x; i < nk * kLines; i += blockDim.x) {
-    const int bk = i / kLines, l = i - bk * kLines;
-    const int b = kept_index(bk, nk, A.R, N);
-    buf0[l * ls + b] = g[(int64_t)bk * A.Cp + l];
-  }
-  __syncthreads();
-  const float2* res = fft_lines<NC, kLines>(buf0, buf1, pl, tw);
-  float2* h = A.Hh + (((int64_t)s * N + x) * N) * A.Cp + c0;
-  for (int i = threadIdx.x; i < kLines * N; i += blockDim.x) {
-    const int y = i / kLines, l = i - y * kLines;
-    h[(int64_t)y * A.Cp + l] = res[l * ls + y];
+  // thread's inputs: i = threadIdx.x + k kThreads -> (bk = i / kLines, l = i % kLines)
+  float2 pre[kYPf];
+  auto src = [&](int u) {
+    const int s = u / (N * nrun), r = u - s * (N * nrun);
+    const int x = r / nrun, c0 = (r - x * nrun) * kLines;
+    return A.G + (((int64_t)s * N + x) * nk) * A.Cp + c0;
+  };
+  auto fetch = [&](int u) {
+    const float2* g = src(u);
+#pragma unroll
+    for (int k = 0; k < kYPf; ++k) {
+      const int i = threadIdx.x + k * kThreads;
+      const int bk = i / kLines, l = i - bk * kLines;
+      pre[k] = bk < nk ? g[(int64_t)bk * A.Cp + l] : make_float2(0.f, 0.f);
+    }
+  };
+  int u = blockIdx.x;
+  if (u < units) fetch(u);
+  for (; u < units; u += gridDim.x) {
+    const float2* g = src(u);
+    // kept frequencies (|q_b| <= R, or all) from the prefetch, the rest of the line zero
+#pragma unroll
+    for (int k = 0; k < kYPf; ++k) {
+      const int i = threadIdx.x + k * kThreads;
+      const int bk = i / kLines, l = i - bk * kLines;
+      if (bk < nk) buf0[l * ls + kept_index(bk, nk, A.R, N)] = pre[k];
+    }
+    for (int i = threadIdx.x + kYPf * kThreads; i < nk * kLines; i += kThreads) {
+      const int bk = i / kLines, l = i - bk * kLines;
+      buf0[l * ls + kept_index(bk, nk, A.R, N)] = g[(int64_t)bk * A.Cp + l];
+    }
+    if (nk < N) {
+      for (int i = threadIdx.x; i < (N - nk) * kLines; i += kThreads) {
+        const int b = A.R + 1 + i / kLines, l = i % kLines;
+        buf0[l * ls + b] = make_float2(0.f, 0.f);
+      }
+    }
+    __syncthreads();
+    if (u + (int)gridDim.x < units) fetch(u + gridDim.x);
+    const float2* res = fft_lines<NC, kLines>(buf0, buf1, pl, tw);
+    const int s = u / (N * nrun), r = u - s * (N * nrun);
+    const int x = r / nrun, c0 = (r - x * nrun) * kLines;
+    float2* h = A.Hh + (((int64_t)s * N + x) * N) * A.Cp + c0;
+    for (int i = threadIdx.x; i < kLines * N; i += kThreads) {
+      const int y = i / kLines, l = i - y * kLines;
+      h[(int64_t)y * A.Cp + l] = res[l * ls + y];
+    }
+    __syncthreads();
   }
 }
 
-// Z pass: block (x, run of 2 kZLines rows y, shell).  Line l packs rows y0 + 2l, y0 + 2l + 1.
+// Z pass: unit (x, run of 2 kZLines rows y, shell).  Line l packs rows y0 + 2l, y0 + 2l + 1.
 template <int NC>
-__global__ void __launch_bounds__(kThreads) synth_z_kernel(SynthArgs A, FftPlan pl) {
+__global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPlan pl, int units) {
   extern __shared__ float2 sm[];
   const int N = NC ? NC : A.N;
   const int ls = line_stride(N);
   float2* buf0 = sm;
   float2* buf1 = buf0 + kZLines * ls;
   float2* tw = buf1 + kZLines * ls;
-  const int x = blockIdx.x;
-  const int y0 = blockIdx.y * 2 * kZLines;
-  const int s = blockIdx.z;
+  const int ny = (N + 2 * kZLines - 1) / (2 * kZLines);
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = A.tw[i];
-  for (int i = threadIdx.x; i < kZLines * ls; i += blockDim.x) buf0[i] = make_float2(0.f, 0.f);
-  __syncthreads();
   const int cn = min(A.R, N / 2) + 1;  // q_c = 0 .. cn - 1 can be nonzero
-  const float2* h = A.Hh + (((int64_t)s * N + x) * N + y0) * A.Cp;
-  {
-    // kThreads / kZLines threads per line, q_c strided by that
-    constexpr int tpl = kThreads / kZLines;
-    const int l = threadIdx.x / tpl;
+  // kThreads / kZLines threads per line, q_c strided by that
+  constexpr int tpl = kThreads / kZLines;
+  const int l = threadIdx.x / tpl, cl = threadIdx.x % tpl;
+  float2 p1[kZPf], p2[kZPf];
+  auto fetch = [&](int u) {
+    const int s = u / (N * ny), r = u - s * (N * ny);
+    const int x = r / ny, y1 = (r - x * ny) * 2 * kZLines + 2 * l;
+    const float2* h = A.Hh + (((int64_t)s * N + x) * N + y1) * A.Cp;
+#pragma unroll
+    for (int k = 0; k < kZPf; ++k) {
+      const int c = cl + k * tpl;
+      p1[k] = (y1 < N && c < cn) ? h[c] : make_float2(0.f, 0.f);
+      p2[k] = (y1 + 1 < N && c < cn) ? h[A.Cp + c] : make_float2(0.f, 0.f);
+    }
+  };
+  // line value at q_c = c and its Hermitian partner at N - c
+  auto put = [&](float2* line, int c, float2 z1, float2 z2) {
+    if (c == 0 || 2 * c == N) {
+      line[c] = make_float2(z1.x, z2.x);
+    } else {
+      line[c] = make_float2(z1.x - z2.y, z1.y + z2.x);       // Z1 + i Z2
+      line[N - c] = make_float2(z1.x + z2.y, -z1.y + z2.x);  // conj(Z1) + i conj(Z2)
+    }
+  };
+  int u = blockIdx.x;
+  if (u < units) fetch(u);
+  for (; u < units; u += gridDim.x) {
+    const int s = u / (N * ny), r = u - s * (N * ny);
+    const int x = r / ny, y0 = (r - x * ny) * 2 * kZLines;
     const int y1 = y0 + 2 * l;
     float2* line = buf0 + l * ls;
-    if (y1 < N) {
-      for (int c = threadIdx.x % tpl; c < cn; c += tpl) {
-        const float2 z1 = h[(int64_t)(2 * l) * A.Cp + c];
-        const float2 z2 =
-            (y1 + 1 < N) ? h[(int64_t)(2 * l + 1) * A.Cp + c] : make_float2(0.f, 0.f);
-        if (c == 0 || 2 * c == N) {
-          line[c] = make_float2(z1.x, z2.x);
-        } else {
-          line[c] = make_float2(z1.x - z2.y, z1.y + z2.x);       // Z1 + i Z2
-          line[N - c] = make_float2(z1.x + z2.y, -z1.y + z2.x);  // conj(Z1) + i conj(Z2)
-        }
+#pragma unroll
+    for (int k = 0; k < kZPf; ++k) {
+      const int c = cl + k * tpl;
+      if (c < cn) put(line, c, p1[k], p2[k]);
+    }
+    if (cn > kZPf * tpl) {
+      const float2* h = A.Hh + (((int64_t)s * N + x) * N + y1) * A.Cp;
+      for (int c = cl + kZPf * tpl; c < cn; c += tpl) {
+        const float2 z1 = y1 < N ? h[c] : make_float2(0.f, 0.f);
+        const float2 z2 = y1 + 1 < N ? h[A.Cp + c] : make_float2(0.f, 0.f);
+        put(line, c, z1, z2);
       }
     }
-  }
-  __syncthreads();
-  const float2* res = fft_lines<NC, kZLines>(buf0, buf1, pl, tw);
-  const int64_t K = (int64_t)N * N * N;
-  const int64_t base = (int64_t)(A.s0 + s - A.out0) * K + ((int64_t)x * N) * N;
-  // four consecutive z per thread: 16-byte field stores, 8-byte hi / lo stores (N % 4 == 0)
-  const int nq = N / 4;
-  for (int i = threadIdx.x; i < 2 * kZLines * nq; i += blockDim.x) {
-    const int r = i / nq, z = (i - r * nq) * 4;  // output row y0 + r
-    const int y = y0 + r;
-    if (y >= N) continue;
-    const float2* w = res + (r >> 1) * ls + z;
-    float4 v;
-    if (r & 1) v = make_float4(w[0].y, w[1].y, w[2].y, w[3].y);
-    else v = make_float4(w[0].x, w[1].x, w[2].x, w[3].x);
-    const int64_t o = base + (int64_t)y * N + z;
-    *reinterpret_cast<float4*>(A.fields + o) = v;
-    if (A.hi) {
-      const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y);
-      const __nv_bfloat162 h23 = __floats2bfloat162_rn(v.z, v.w);
-      const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
-      const __nv_bfloat162 l01 = __floats2bfloat162_rn(v.x - f01.x, v.y - f01.y);
-      const __nv_bfloat162 l23 = __floats2bfloat162_rn(v.z - f23.x, v.w - f23.y);
-      uint2 hv, lv;
-      hv.x = *reinterpret_cast<const uint32_t*>(&h01);
-      hv.y = *reinterpret_cast<const uint32_t*>(&h23);
-      lv.x = *reinterpret_cast<const uint32_t*>(&l01);
-      lv.y = *reinterpret_cast<const uint32_t*>(&l23);
-      *reinterpret_cast<uint2*>(A.hi + o) = hv;
-      *reinterpret_cast<uint2*>(A.lo + o) = lv;
+    for (int c = cn + cl; c <= N - cn; c += tpl) line[c] = make_float2(0.f, 0.f);
+    __syncthreads();
+    if (u + (int)gridDim.x < units) fetch(u + gridDim.x);
+    const float2* res = fft_lines<NC, kZLines>(buf0, buf1, pl, tw);
+    const int64_t K = (int64_t)N * N * N;
+    const int64_t base = (int64_t)(A.s0 + s - A.out0) * K + ((int64_t)x * N) * N;
+    // four consecutive z per thread: 16-byte field stores, 8-byte hi / lo stores (N % 4 == 0)
+    const int nq = N / 4;
+    for (int i = threadIdx.x; i < 2 * kZLines * nq; i += kThreads) {
+      const int rr = i / nq, z = (i - rr * nq) * 4;  // output row y0 + rr
+      const int y = y0 + rr;
+      if (y >= N) continue;
+      const float2* w = res + (rr >> 1) * ls + z;
+      float4 v;
+      if (rr & 1) v = make_float4(w[0].y, w[1].y, w[2].y, w[3].y);
+      else v = make_float4(w[0].x, w[1].x, w[2].x, w[3].x);
+      const int64_t o = base + (int64_t)y * N + z;
+      *reinterpret_cast<float4*>(A.fields + o) = v;
+      if (A.hi) {
+        const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y);
+        const __nv_bfloat162 h23 = __floats2bfloat162_rn(v.z, v.w);
+        const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
+        const __nv_bfloat162 l01 = __floats2bfloat162_rn(v.x - f01.x, v.y - f01.y);
+        const __nv_bfloat162 l23 = __floats2bfloat162_rn(v.z - f23.x, v.w - f23.y);
+        uint2 hv, lv;
+        hv.x = *reinterpret_cast<const uint32_t*>(&h01);
+        hv.y = *reinterpret_cast<const uint32_t*>(&h23);
+        lv.x = *reinterpret_cast<const uint32_t*>(&l01);
+        lv.y = *reinterpret_cast<const uint32_t*>(&l23);
+        *reinterpret_cast<uint2*>(A.hi + o) = hv;
+        *reinterpret_cast<uint2*>(A.lo + o) = lv;
+      }
     }
+    __syncthreads();
   }
 }
 
@@ -459,11 +521,21 @@ void run_synth(const SynthArgs& A, const FftPlan& pl, int nk, int Cp, int ns, si
   const int N = A.N;
   synth_x_kernel<NC><<<dim3(nk, Cp / kLines), kThreads, x_smem, st>>>(A, pl);
   BSK_CHECK_CUDA(cudaGetLastError());
-  synth_y_kernel<NC><<<dim3(N, Cp / kLines, ns), kThreads, fft_smem, st>>>(A, pl);
-  BSK_CHECK_CUDA(cudaGetLastError());
+  // persistent Y and Z passes: as many blocks as are resident at once
+  int nsm = 0, by = 0, bz = 0;
+  BSK_CHECK_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const size_t z_smem = (2 * (size_t)kZLines * (N + 1) + N) * sizeof(float2);
-  synth_z_kernel<NC><<<dim3(N, (N + 2 * kZLines - 1) / (2 * kZLines), ns), kThreads, z_smem, st>>>(
-      A, pl);
+  BSK_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by, synth_y_kernel<NC>, kThreads,
+                                                               fft_smem));
+  BSK_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bz, synth_z_kernel<NC>, kThreads,
+                                                               z_smem));
+  const int y_units = N * (Cp / kLines) * ns;
+  const int z_units = N * ((N + 2 * kZLines - 1) / (2 * kZLines)) * ns;
+  const int y_grid = std::max(1, std::min(y_units, std::max(by, 1) * nsm));
+  const int z_grid = std::max(1, std::min(z_units, std::max(bz, 1) * nsm));
+  synth_y_kernel<NC><<<y_grid, kThreads, fft_smem, st>>>(A, pl, y_units);
+  BSK_CHECK_CUDA(cudaGetLastError());
+  synth_z_kernel<NC><<<z_grid, kThreads, z_smem, st>>>(A, pl, z_units);
   BSK_CHECK_CUDA(cudaGetLastError());
 }
 
