@@ -184,6 +184,15 @@ __host__ __device__ constexpr int plan_np(int n) {
 // writes of a warp on distinct banks.
 __host__ __device__ constexpr int line_stride(int n) { return n + 1; }
 
+template <int R>
+__device__ __forceinline__ void dft_radix(float2* v, const FftPlan& pl) {
+  if (R == 16) dft16(v);
+  else if (R == 24) dft_comp<8, 3>(v, pl);
+  else if (R == 12) dft_comp<4, 3>(v, pl);
+  else if (R == 6) dft_comp<2, 3>(v, pl);
+  else dft_small<R>(v, pl);
+}
+
 // One Stockham pass of radix R over `lines` sequences of length n (src -> dst).
 template <int R>
 __device__ __forceinline__ void fft_pass(const float2* __restrict__ src, float2* __restrict__ dst,
@@ -205,11 +214,7 @@ __device__ __forceinline__ void fft_pass(const float2* __restrict__ src, float2*
 #pragma unroll
       for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * step]);
     }
-    if (R == 16) dft16(v);
-    else if (R == 24) dft_comp<8, 3>(v, pl);
-    else if (R == 12) dft_comp<4, 3>(v, pl);
-    else if (R == 6) dft_comp<2, 3>(v, pl);
-    else dft_small<R>(v, pl);
+    dft_radix<R>(v, pl);
     const int idx = (j / Ns) * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) o[idx + r * Ns] = v[r];
@@ -228,6 +233,22 @@ __device__ __forceinline__ void run_passes(float2*& src, float2*& dst,
     src = dst;
     dst = t2;
     run_passes<N, L, P + 1, Ns * R>(src, dst, tw, pl);
+  }
+}
+
+// All passes but the last (the Z pass fuses the last one with its stores).
+template <int N, int L, int P, int Ns>
+__device__ __forceinline__ void run_passes_but_last(float2*& src, float2*& dst,
+                                                    const float2* __restrict__ tw,
+                                                    const FftPlan& pl) {
+  if constexpr (P + 1 < plan_np(N)) {
+    constexpr int R = plan_radix(N, P);
+    fft_pass<R>(src, dst, L, N, Ns, tw, pl);
+    __syncthreads();
+    float2* t2 = src;
+    src = dst;
+    dst = t2;
+    run_passes_but_last<N, L, P + 1, Ns * R>(src, dst, tw, pl);
   }
 }
 
@@ -409,6 +430,51 @@ __global__ void __launch_bounds__(kThreads, 2) synth_y_kernel(SynthArgs A, FftPl
   }
 }
 
+// Last FFT pass of the Z pass fused with its stores.  Butterfly j of a line yields the
+// outputs z = j + M r (M = n / R); lanes j (even) and j + 1 hold z and z + 1, so one
+// exchange gives the even lane row y1's pair (z, z + 1) (real parts) and the odd lane row
+// y2's (imaginary parts): 8-byte field stores, 4-byte hi / lo stores, 32-byte sectors.
+template <int NC>
+__device__ __forceinline__ void z_last_pass(const float2* __restrict__ src,
+                                            const float2* __restrict__ tw, const FftPlan& pl,
+                                            const SynthArgs& A, int64_t base, int y0) {
+  constexpr int np = plan_np(NC);
+  constexpr int R = plan_radix(NC, np - 1);
+  constexpr int M = NC / R;
+  static_assert(np >= 2 && M % 2 == 0 && (kZLines * M) % kThreads == 0,
+                "the fused last pass wants full warps of line-ordered butterfly pairs");
+  constexpr int ls = line_stride(NC);
+  for (int t = threadIdx.x; t < kZLines * M; t += kThreads) {
+    const int line = t / M, j = t - line * M;
+    const float2* in = src + line * ls;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = in[j + r * M];
+#pragma unroll
+    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * j]);
+    dft_radix<R>(v, pl);
+    const bool odd = j & 1;
+    const int y = y0 + 2 * line + (odd ? 1 : 0);
+    const int64_t o = base + (int64_t)y * NC + (j & ~1);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const float got = __shfl_xor_sync(0xffffffffu, odd ? v[r].x : v[r].y, 1);
+      const float2 f = odd ? make_float2(got, v[r].y) : make_float2(v[r].x, got);
+      if (y < NC) {
+        const int64_t p = o + (int64_t)M * r;
+        *reinterpret_cast<float2*>(A.fields + p) = f;
+        if (A.hi) {
+          const __nv_bfloat162 h = __floats2bfloat162_rn(f.x, f.y);
+          const float2 fb = __bfloat1622float2(h);
+          const __nv_bfloat162 lw = __floats2bfloat162_rn(f.x - fb.x, f.y - fb.y);
+          *reinterpret_cast<__nv_bfloat162*>(A.hi + p) = h;
+          *reinterpret_cast<__nv_bfloat162*>(A.lo + p) = lw;
+        }
+      }
+    }
+  }
+}
+
 // Z pass: unit (x, run of 2 kZLines rows y, shell).  Line l packs rows y0 + 2l, y0 + 2l + 1.
 template <int NC>
 __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPlan pl, int units) {
@@ -468,34 +534,41 @@ __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPl
     for (int c = cn + cl; c <= N - cn; c += tpl) line[c] = make_float2(0.f, 0.f);
     __syncthreads();
     if (u + (int)gridDim.x < units) fetch(u + gridDim.x);
-    const float2* res = fft_lines<NC, kZLines>(buf0, buf1, pl, tw);
     const int64_t K = (int64_t)N * N * N;
     const int64_t base = (int64_t)(A.s0 + s - A.out0) * K + ((int64_t)x * N) * N;
-    // four consecutive z per thread: 16-byte field stores, 8-byte hi / lo stores (N % 4 == 0)
-    const int nq = N / 4;
-    for (int i = threadIdx.x; i < 2 * kZLines * nq; i += kThreads) {
-      const int rr = i / nq, z = (i - rr * nq) * 4;  // output row y0 + rr
-      const int y = y0 + rr;
-      if (y >= N) continue;
-      const float2* w = res + (rr >> 1) * ls + z;
-      float4 v;
-      if (rr & 1) v = make_float4(w[0].y, w[1].y, w[2].y, w[3].y);
-      else v = make_float4(w[0].x, w[1].x, w[2].x, w[3].x);
-      const int64_t o = base + (int64_t)y * N + z;
-      *reinterpret_cast<float4*>(A.fields + o) = v;
-      if (A.hi) {
-        const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y);
-        const __nv_bfloat162 h23 = __floats2bfloat162_rn(v.z, v.w);
-        const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
-        const __nv_bfloat162 l01 = __floats2bfloat162_rn(v.x - f01.x, v.y - f01.y);
-        const __nv_bfloat162 l23 = __floats2bfloat162_rn(v.z - f23.x, v.w - f23.y);
-        uint2 hv, lv;
-        hv.x = *reinterpret_cast<const uint32_t*>(&h01);
-        hv.y = *reinterpret_cast<const uint32_t*>(&h23);
-        lv.x = *reinterpret_cast<const uint32_t*>(&l01);
-        lv.y = *reinterpret_cast<const uint32_t*>(&l23);
-        *reinterpret_cast<uint2*>(A.hi + o) = hv;
-        *reinterpret_cast<uint2*>(A.lo + o) = lv;
+    if constexpr (NC != 0) {
+      float2* src = buf0;
+      float2* dst = buf1;
+      run_passes_but_last<NC, kZLines, 0, 1>(src, dst, tw, pl);
+      z_last_pass<NC>(src, tw, pl, A, base, y0);
+    } else {
+      const float2* res = fft_lines<NC, kZLines>(buf0, buf1, pl, tw);
+      // four consecutive z per thread: 16-byte field stores, 8-byte hi / lo stores (N % 4 == 0)
+      const int nq = N / 4;
+      for (int i = threadIdx.x; i < 2 * kZLines * nq; i += kThreads) {
+        const int rr = i / nq, z = (i - rr * nq) * 4;  // output row y0 + rr
+        const int y = y0 + rr;
+        if (y >= N) continue;
+        const float2* w = res + (rr >> 1) * ls + z;
+        float4 v;
+        if (rr & 1) v = make_float4(w[0].y, w[1].y, w[2].y, w[3].y);
+        else v = make_float4(w[0].x, w[1].x, w[2].x, w[3].x);
+        const int64_t o = base + (int64_t)y * N + z;
+        *reinterpret_cast<float4*>(A.fields + o) = v;
+        if (A.hi) {
+          const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y);
+          const __nv_bfloat162 h23 = __floats2bfloat162_rn(v.z, v.w);
+          const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
+          const __nv_bfloat162 l01 = __floats2bfloat162_rn(v.x - f01.x, v.y - f01.y);
+          const __nv_bfloat162 l23 = __floats2bfloat162_rn(v.z - f23.x, v.w - f23.y);
+          uint2 hv, lv;
+          hv.x = *reinterpret_cast<const uint32_t*>(&h01);
+          hv.y = *reinterpret_cast<const uint32_t*>(&h23);
+          lv.x = *reinterpret_cast<const uint32_t*>(&l01);
+          lv.y = *reinterpret_cast<const uint32_t*>(&l23);
+          *reinterpret_cast<uint2*>(A.hi + o) = hv;
+          *reinterpret_cast<uint2*>(A.lo + o) = lv;
+        }
       }
     }
     __syncthreads();

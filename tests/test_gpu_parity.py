@@ -111,10 +111,11 @@ def test_gridinfo_exact_vs_oracle(cuda, grid):
     assert np.allclose(km[ok], kmo[ok], rtol=1e-12, atol=0)
 
 
-@pytest.mark.parametrize("n", [32, 40, 56])
+@pytest.mark.parametrize("n", [32, 40, 48, 56, 96])
 def test_fields_match_oracle_native(cuda, n):
-    # 32 and 40: the field synthesis (compile-time-free plans 16x2, 8x5); 56 = 8 x 7 has no
-    # synthesis plan and takes the filter + cuFFT C2R path
+    # 32 and 40: the field synthesis with run-time plans (16x2, 8x5); 48 and 96: compile-time
+    # plans (16x3, 16x6) whose last pass writes the fields straight from registers; 56 = 8 x 7
+    # has no synthesis plan and takes the filter + cuFFT C2R path
     n, box, edges, _ = _small(n, 100.0, 2)
     delta = synthetic.lognormal_mesh(n, box, seed=11)
     plan = Plan(n, box, edges, grid="native")
