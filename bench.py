@@ -433,7 +433,7 @@ def run_ours(args):
         line["speedup_vs_fp32_plain"] = value / fp32["value"]
     if args.serve_requests > 0 and world == 1:
         plan.close()
-        del delta, host, dmesh
+        del delta, host, bufs
         torch.cuda.empty_cache()
         line["serving"] = run_serving(args, dev)
         if not args.no_fp32:
