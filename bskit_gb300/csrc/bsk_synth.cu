@@ -10,7 +10,8 @@
 //           q_c packed as Z1 + i Z2 -> one complex inverse FFT whose real and imaginary
 //           parts are the two real output rows; the rows are written as FP32 fields and,
 //           when asked, as the bf16 hi / lo planes of the tensor-core contraction.
-// Every array keeps q_c fastest, so each pass reads and writes 16-wide (128-byte) runs.
+// Every array keeps q_c fastest, so the passes read and write 8- or 16-wide (64- or 128-byte)
+// runs of it.
 // The FFTs are radix-8/4/2/3/5 Stockham passes in shared memory (twiddles from a table
 // computed in double precision on the host); unnormalised, sign +1, as cuFFT's C2R.
 #include <cmath>
@@ -20,7 +21,9 @@
 namespace bsk {
 namespace {
 
-constexpr int kLines = 16;   // lines (one 16-wide q_c run) per block of the X and Y passes
+constexpr int kLines = 16;   // lines (one 16-wide q_c run) per block of the Y pass
+constexpr int kXLines = 8;   // X pass: half a q_c run per block (its staged spectrum columns
+                             // need shared memory too; 8 lines let three blocks share an SM)
 constexpr int kZLines = 16;  // lines (two output rows each) per block of the Z pass
 constexpr int kThreads = 256;
 
@@ -313,17 +316,17 @@ __global__ void __launch_bounds__(kThreads) synth_x_kernel(SynthArgs A, FftPlan 
   extern __shared__ float2 sm[];
   const int N = NC ? NC : A.N, nk = A.nk;
   const int ls = line_stride(N);
-  float2* buf0 = sm;                       // kLines lines
-  float2* buf1 = buf0 + kLines * ls;       // kLines lines
-  float2* tw = buf1 + kLines * ls;         // N
-  float2* sS = tw + N;                     // nk * kLines
-  uint16_t* sT = reinterpret_cast<uint16_t*>(sS + nk * kLines);  // nk * kLines
+  float2* buf0 = sm;                       // kXLines lines
+  float2* buf1 = buf0 + kXLines * ls;       // kXLines lines
+  float2* tw = buf1 + kXLines * ls;         // N
+  float2* sS = tw + N;                     // nk * kXLines
+  uint16_t* sT = reinterpret_cast<uint16_t*>(sS + nk * kXLines);  // nk * kXLines
   const int bk = blockIdx.x;
-  const int c0 = blockIdx.y * kLines;
+  const int c0 = blockIdx.y * kXLines;
   const int b = kept_index(bk, nk, A.R, N);
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = A.tw[i];
-  for (int i = threadIdx.x; i < nk * kLines; i += blockDim.x) {
-    const int ak = i / kLines, l = i - ak * kLines;
+  for (int i = threadIdx.x; i < nk * kXLines; i += blockDim.x) {
+    const int ak = i / kXLines, l = i - ak * kXLines;
     const int a = kept_index(ak, nk, A.R, N);
     const int c = c0 + l;
     float2 v = make_float2(0.f, 0.f);
@@ -338,23 +341,23 @@ __global__ void __launch_bounds__(kThreads) synth_x_kernel(SynthArgs A, FftPlan 
   }
   __syncthreads();
   for (int s = 0; s < A.ns; ++s) {
-    for (int i = threadIdx.x; i < kLines * N; i += blockDim.x) {
-      const int a = i / kLines, l = i - a * kLines;
+    for (int i = threadIdx.x; i < kXLines * N; i += blockDim.x) {
+      const int a = i / kXLines, l = i - a * kXLines;
       // position a of line l holds frequency index a
       const int qa = fft_freq(a, N);
       float2 v = make_float2(0.f, 0.f);
       if (nk == N || (qa >= -A.R && qa <= A.R)) {
         const int ak = nk == N ? a : qa + A.R;
-        if (in_shell(sT[ak * kLines + l], A.s0 + s)) v = sS[ak * kLines + l];
+        if (in_shell(sT[ak * kXLines + l], A.s0 + s)) v = sS[ak * kXLines + l];
       }
       buf0[l * ls + a] = v;
     }
     __syncthreads();
-    const float2* res = fft_lines<NC, kLines>(buf0, buf1, pl, tw);
+    const float2* res = fft_lines<NC, kXLines>(buf0, buf1, pl, tw);
     // G[s][x][bk][c0 + l]
     float2* g = A.G + (((int64_t)s * N) * nk + bk) * A.Cp + c0;
-    for (int i = threadIdx.x; i < kLines * N; i += blockDim.x) {
-      const int x = i / kLines, l = i - x * kLines;
+    for (int i = threadIdx.x; i < kXLines * N; i += blockDim.x) {
+      const int x = i / kXLines, l = i - x * kXLines;
       g[(int64_t)x * nk * A.Cp + l] = res[l * ls + x];
     }
     __syncthreads();
@@ -592,7 +595,7 @@ void run_synth(const SynthArgs& A, const FftPlan& pl, int nk, int Cp, int ns, si
     attr_done[dev] = true;
   }
   const int N = A.N;
-  synth_x_kernel<NC><<<dim3(nk, Cp / kLines), kThreads, x_smem, st>>>(A, pl);
+  synth_x_kernel<NC><<<dim3(nk, Cp / kXLines), kThreads, x_smem, st>>>(A, pl);
   BSK_CHECK_CUDA(cudaGetLastError());
   // persistent Y and Z passes: as many blocks as are resident at once
   int nsm = 0, by = 0, bz = 0;
@@ -679,7 +682,8 @@ void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0
   A.lo = lo;
   A.tw = tw;
   const size_t fft_smem = (2 * (size_t)kLines * (N + 1) + N) * sizeof(float2);
-  const size_t x_smem = fft_smem + (size_t)nk * kLines * (sizeof(float2) + sizeof(uint16_t));
+  const size_t x_smem = (2 * (size_t)kXLines * (N + 1) + N) * sizeof(float2) +
+                        (size_t)nk * kXLines * (sizeof(float2) + sizeof(uint16_t));
   BSK_REQUIRE(x_smem <= 227 * 1024, BSK_ERR_UNSUPPORTED, "grid too large for the field synthesis");
   switch (N) {
     case 48: run_synth<48>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
