@@ -10,7 +10,10 @@
 //     64-point K block as one 128-row operand (rows 0..63 hi, 64..127 lo;
 //     SWIZZLE_128B, K-major), and the FP32 tile(s) of the pair-factor shells
 //     (one tile when one range covers both factors of every row, as for auto
-//     spectra), each with only as many shell rows (16/32/48/64) as the tile uses;
+//     spectra), each with only as many shell rows (16/32/48/64) as the tile uses.
+//     A stage's source tiles are refilled as soon as the A-operand warps have read
+//     them and its B tiles once the stage's MMAs completed, each part with its own
+//     "landed" barrier, so the sources get about one more stage of lead time;
 //   * warps 10..17 (2 per TMEM lane quadrant, one 64-point half each) read the
 //     row's F1_i, F2_j from SMEM, form P = F1_i*F2_j with packed f32x2
 //     arithmetic, split P = hi + lo (bf16 round-to-nearest) and store them with
@@ -27,8 +30,8 @@
 //     of the slice add the entries that are triangle bins into the FP64 output
 //     (atomics).
 // The MMAs' completion is committed once per stage, to a ring of mbarriers that
-// the TMA producer (SMEM stage free), the A-operand warps (TMEM A stage free) and the
-// drain (accumulator ready) all wait on.  Stages are 128 points long so that the fixed
+// the TMA producer (the stage's B tiles free), the A-operand warps (TMEM A stage free)
+// and the drain (accumulator ready) all wait on.  Stages are 128 points long so that the fixed
 // cost of a stage's barrier round trips is spread over 16 MMAs.  Every wait is bounded
 // (globaltimer); on expiry the kernel records an error flag, stops issuing work, drains
 // its own MMAs and frees TMEM.
@@ -65,7 +68,7 @@ template <bool kTwoSrc> struct Ring {
 constexpr int MAX_SSTAGES = 3;
 
 // One commit per stage serves every consumer of "the stage's MMAs are complete": the TMA
-// producer (SMEM stage free, SST stages later), the A-operand warps (TMEM A stage free,
+// producer (the stage's B tiles free, SST stages later), the A-operand warps (TMEM A stage free,
 // ASTAGES later) and the drain (accumulator ready, the same stage).  DONE_RING > all of
 // those distances, so no barrier of the ring completes twice before each of its waiters
 // has seen the phase (each waiter's progress gates the MMA thread's).
@@ -73,7 +76,9 @@ constexpr int DONE_RING = 4;
 static_assert(ACC_CHUNKS == 1, "the drain waits on the per-stage completion");
 
 struct Bars {
-  uint64_t full[MAX_SSTAGES];      // TMA bytes landed
+  uint64_t full[MAX_SSTAGES];      // the stage's source tiles landed (TMA bytes)
+  uint64_t full_b[MAX_SSTAGES];    // the stage's B tiles landed (TMA bytes)
+  uint64_t src_free[MAX_SSTAGES];  // the A-operand warps have read the stage's sources (8)
   uint64_t done[DONE_RING];        // the MMAs of stage c completed (tcgen05.commit), c % 4
   uint64_t afull[ASTAGES];         // A operand of the chunk is in TMEM (8 warp arrivals)
   uint64_t accempty[NACC];
@@ -331,6 +336,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < SST; ++s) {
       mbar_init(&bars->full[s], 1);
+      mbar_init(&bars->full_b[s], 1);
+      mbar_init(&bars->src_free[s], 8);
 
     }
     for (int a = 0; a < ASTAGES; ++a) {
@@ -369,27 +376,26 @@ __global__ void __launch_bounds__(THREADS, 1)
         const bool one_src = !kTwoSrc || (same_src && td.i0 == td.j0);
         const int64_t x_begin = k_begin + sl * SLICE;
         const int64_t x_end = min(k_end, x_begin + SLICE);
-        // bytes per stage: the column rows of hi and lo in both K blocks, the four
-        // 32-point quarters of each source tile
-        const uint32_t bytes =
-            (uint32_t)(4 * box_rows(td.nc) * 128 +
-                       4 * 128 * (box_rows(td.ni) + (one_src ? 0 : box_rows(td.nj))));
+        // bytes per stage: the four 32-point quarters of each source tile; the column rows
+        // of hi and lo in both K blocks
+        const uint32_t src_bytes =
+            (uint32_t)(4 * 128 * (box_rows(td.ni) + (one_src ? 0 : box_rows(td.nj))));
+        const uint32_t b_bytes = (uint32_t)(4 * box_rows(td.nc) * 128);
         for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
           const int s = chunk % SST;
-          // SMEM stage s was last read by the MMAs of stage chunk - SST
-          if (chunk >= SST && !mbar_wait(&bars->done[(chunk - SST) % DONE_RING],
-                                          ((chunk - SST) / DONE_RING) & 1)) {
+          const uint32_t st = sbase + s * STAGE_BYTES;
+          const int xi = (int)x;
+          // The source tiles of SMEM stage s were last read by the A-operand warps of stage
+          // chunk - SST, its B tiles by that stage's MMAs, which complete ~one A-operand
+          // stage later: the sources are refilled as soon as they are free.
+          if (chunk >= SST &&
+              !mbar_wait(&bars->src_free[s], (uint32_t)((chunk - SST) / SST) & 1)) {
             ok = false;
             break;
           }
-          mbar_arrive_tx(&bars->full[s], bytes);
-          const uint32_t st = sbase + s * STAGE_BYTES;
-          const int xi = (int)x;
+          mbar_arrive_tx(&bars->full[s], src_bytes);
           if (fused) {
-            // one copy for B (both 64-point blocks, hi and lo: [block][plane][nc rows]),
-            // one per source tile ([32-point block][rows])
-            tma_load_4d(st, by_rows(td.nc, &maps.b16, &maps.b32, &maps.b48, &maps.b64),
-                        &bars->full[s], 0, td.l0, 0, xi / KBLK);
+            // one copy per source tile ([32-point block][rows])
             tma_load_3d(st + 2 * B_BLOCK,
                         by_rows(td.ni, &maps.a1_16, &maps.a1_32, &maps.a1_48, &maps.a1_64),
                         &bars->full[s], 0, td.i0, xi / 32);
@@ -398,18 +404,30 @@ __global__ void __launch_bounds__(THREADS, 1)
                           by_rows(td.nj, &maps.a2_16, &maps.a2_32, &maps.a2_48, &maps.a2_64),
                           &bars->full[s], 0, td.j0, xi / 32);
           } else {
-            for (int kb = 0; kb < KCH / KBLK; ++kb) {
-              load_rows(st + kb * B_BLOCK, &maps.hi16, &maps.hi32, &maps.hi64, &bars->full[s],
-                        xi + KBLK * kb, td.l0, td.nc);
-              load_rows(st + kb * B_BLOCK + B_TILE, &maps.lo16, &maps.lo32, &maps.lo64,
-                        &bars->full[s], xi + KBLK * kb, td.l0, td.nc);
-            }
             for (int q = 0; q < 4; ++q) {
               load_rows(st + 2 * B_BLOCK + q * A_QUARTER, &maps.f1_16, &maps.f1_32, &maps.f1_64,
                         &bars->full[s], xi + 32 * q, td.i0, td.ni);
               if (!one_src)
                 load_rows(st + 2 * B_BLOCK + A_TILE + q * A_QUARTER, &maps.f2_16, &maps.f2_32,
                           &maps.f2_64, &bars->full[s], xi + 32 * q, td.j0, td.nj);
+            }
+          }
+          if (chunk >= SST && !mbar_wait(&bars->done[(chunk - SST) % DONE_RING],
+                                          ((chunk - SST) / DONE_RING) & 1)) {
+            ok = false;
+            break;
+          }
+          mbar_arrive_tx(&bars->full_b[s], b_bytes);
+          if (fused) {
+            // one copy for B (both 64-point blocks, hi and lo: [block][plane][nc rows])
+            tma_load_4d(st, by_rows(td.nc, &maps.b16, &maps.b32, &maps.b48, &maps.b64),
+                        &bars->full_b[s], 0, td.l0, 0, xi / KBLK);
+          } else {
+            for (int kb = 0; kb < KCH / KBLK; ++kb) {
+              load_rows(st + kb * B_BLOCK, &maps.hi16, &maps.hi32, &maps.hi64, &bars->full_b[s],
+                        xi + KBLK * kb, td.l0, td.nc);
+              load_rows(st + kb * B_BLOCK + B_TILE, &maps.lo16, &maps.lo32, &maps.lo64,
+                        &bars->full_b[s], xi + KBLK * kb, td.l0, td.nc);
             }
           }
         }
@@ -442,7 +460,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int a = chunk % ASTAGES;
         const uint32_t pa = (chunk / ASTAGES) & 1;
         if (!__all_sync(0xffffffffu, mbar_wait(&bars->accempty[b], ((grp / NACC) & 1) ^ 1) &&
-                                         mbar_wait(&bars->full[s], ph) &&
+                                         mbar_wait(&bars->full_b[s], ph) &&
                                          mbar_wait(&bars->afull[a], pa))) {
           ok = false;
           break;
@@ -592,7 +610,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&bars->afull[a]);
+        if (lane == 0) {
+          mbar_arrive(&bars->afull[a]);
+          mbar_arrive(&bars->src_free[s]);  // this warp's loads of the stage's sources are done
+        }
       }
     }
   }
