@@ -134,7 +134,7 @@ int64_t footprint(const bsk_plan* p) {
   for (const auto& s : p->slot) {
     if (s.spec) fp += p->Mh * 8;
     if (s.fields) fp += (int64_t)p->n_alloc() * p->K * 4;
-    if (s.hi) fp += (int64_t)p->n_alloc() * p->K * 4;
+    if (s.split) fp += (int64_t)split_elems(p->n_alloc(), p->K) * 2;
   }
   if (p->stream_C) fp += (int64_t)p->stream_C * p->K * (3 * 4 + (p->stream_tc ? 4 : 0));
   if (p->synth_ws) fp += (int64_t)p->synth_ws_bytes;
@@ -163,18 +163,14 @@ void release_stream(bsk_plan* p) {
 }
 
 void alloc_split(bsk_plan* p, FieldSlot& f) {
-  if (f.hi) return;
-  // hi and lo are two planes of one allocation (the contraction loads both with one copy)
-  const size_t n = (size_t)p->n_alloc() * p->K;
-  check_budget(p, n * 2 * sizeof(__nv_bfloat16), "the bf16 split of the fields");
-  f.hi = (__nv_bfloat16*)dmalloc(2 * n * sizeof(__nv_bfloat16));
-  f.lo = f.hi + n;
-  // shells beyond n (padding to the FFT batch) are read by some tiles' boxes: keep them zero
-  const size_t pad = (size_t)(p->n_alloc() - p->n) * p->K;
-  if (pad) {
-    BSK_CHECK_CUDA(cudaMemset(f.hi + (size_t)p->n * p->K, 0, pad * sizeof(__nv_bfloat16)));
-    BSK_CHECK_CUDA(cudaMemset(f.lo + (size_t)p->n * p->K, 0, pad * sizeof(__nv_bfloat16)));
-  }
+  if (f.split) return;
+  // the chunk-major split of all n_alloc shells; zeroed once, so that the shells beyond n
+  // (padding to the FFT batch, read by some tiles' boxes) and the tail of the last chunk
+  // stay zero when only the synthesis writes it
+  const size_t bytes = split_elems(p->n_alloc(), p->K) * sizeof(__nv_bfloat16);
+  check_budget(p, bytes, "the bf16 split of the fields");
+  f.split = (__nv_bfloat16*)dmalloc(bytes);
+  BSK_CHECK_CUDA(cudaMemset(f.split, 0, bytes));
 }
 
 // Masked shell fields of `slot` for every shell.  With a grid the field synthesis
@@ -203,7 +199,7 @@ void ensure_fields(bsk_plan* p, int s, cudaStream_t st, bool with_split = false)
       int R = 0;
       for (int k = s0; k < s0 + ns; ++k) R = std::max(R, p->shell_r[k]);
       launch_synth(p->Ng, f.spec, p->table, s0, ns, R, p->synth_ws, f.fields,
-                   with_split ? f.hi : nullptr, with_split ? f.lo : nullptr, st);
+                   with_split ? f.split : nullptr, p->n_alloc(), st);
     }
     f.fields_ok = true;
     f.split_ok = with_split;
@@ -228,15 +224,14 @@ void ensure_split(bsk_plan* p, int s, cudaStream_t st) {
   ensure_fields(p, s, st, true);
   if (f.split_ok) return;
   alloc_split(p, f);
-  const size_t n = (size_t)p->n_alloc() * p->K;
-  launch_split(f.fields, f.hi, f.lo, (int64_t)n, st);
+  launch_split(f.fields, p->n_alloc(), p->K, f.split, st);
   f.split_ok = true;
 }
 
 void free_slot(FieldSlot& f) {
   if (f.spec) cudaFree(f.spec);
   if (f.fields) cudaFree(f.fields);
-  if (f.hi) cudaFree(f.hi);  // lo is the second plane of the same allocation
+  if (f.split) cudaFree(f.split);
   f = FieldSlot{};
 }
 
@@ -273,7 +268,7 @@ void copy_dups(const bsk_triset* set, double* v, cudaStream_t st) {
 }
 
 void contract_dispatch(bsk_plan* p, const bsk_triset* set, const float* f1, const float* f2,
-                       const float* f3, const __nv_bfloat16* hi, const __nv_bfloat16* lo,
+                       const float* f3, const __nv_bfloat16* split, int split_shells,
                        int64_t K, int64_t k0, int64_t k1, int precision, double* out,
                        cudaStream_t st) {
   BSK_CHECK_CUDA(cudaMemsetAsync(out, 0, (size_t)set->T * sizeof(double), st));
@@ -286,7 +281,7 @@ void contract_dispatch(bsk_plan* p, const bsk_triset* set, const float* f1, cons
       break;
     case BSK_PREC_BF16X3:
     case BSK_PREC_BF16:
-      launch_contract_tc(set->sched, f1, f2, hi, lo, p->n, K, k0, k1,
+      launch_contract_tc(set->sched, f1, f2, split, split_shells, p->n, K, k0, k1,
                          precision == BSK_PREC_BF16X3 ? 3 : 1, out, p->num_sms, st);
       break;
     default:
@@ -345,8 +340,8 @@ void chunk_fields(bsk_plan* p, int slot, int s0, int C, float* dst, cudaStream_t
       }
       int R = 0;
       for (int k = first; k < first + ns; ++k) R = std::max(R, p->shell_r[k]);
-      launch_synth(p->Ng, f.spec, p->table, first, ns, R, p->synth_ws, dst, nullptr, nullptr,
-                   st, s0);
+      launch_synth(p->Ng, f.spec, p->table, first, ns, R, p->synth_ws, dst, nullptr, 0, st,
+                   s0);
       if (ns < p->chunk)
         BSK_CHECK_CUDA(cudaMemsetAsync(dst + (size_t)(b + ns) * p->K, 0,
                                        (size_t)(p->chunk - ns) * p->K * sizeof(float), st));
@@ -397,7 +392,7 @@ void measure_b_stream(bsk_plan* p, const bsk_triset* set, int a, int b, int c, i
   if (C != p->stream_C || (tc && !p->stream_tc)) {
     release_stream(p);
     for (auto& buf : p->stream_f) buf.ptr = dmalloc((size_t)C * p->K * sizeof(float));
-    if (tc) p->stream_split.ptr = dmalloc((size_t)C * p->K * 2 * sizeof(__nv_bfloat16));
+    if (tc) p->stream_split.ptr = dmalloc(split_elems(C, p->K) * sizeof(__nv_bfloat16));
     p->stream_C = C;
     p->stream_tc = tc;
   }
@@ -436,15 +431,14 @@ void measure_b_stream(bsk_plan* p, const bsk_triset* set, int a, int b, int c, i
       for (int r2 = r + 1; r2 < 3; ++r2)
         if (want[r2] == want[r]) fp[r2] = fp[r];
     }
-    const __nv_bfloat16 *hi = nullptr, *lo = nullptr;
+    const __nv_bfloat16* split = nullptr;
     if (tc) {
       __nv_bfloat16* h = (__nv_bfloat16*)p->stream_split.ptr;
       if (p->stream_split.key != want[2]) {
-        launch_split(fp[2], h, h + (size_t)C * p->K, (int64_t)C * p->K, st);
+        launch_split(fp[2], C, p->K, h, st);
         p->stream_split.key = want[2];
       }
-      hi = h;
-      lo = h + (size_t)C * p->K;
+      split = h;
     }
     switch (precision) {
       case BSK_PREC_FP64:
@@ -456,7 +450,7 @@ void measure_b_stream(bsk_plan* p, const bsk_triset* set, int a, int b, int c, i
                                  p->num_sms, st);
         break;
       default:
-        launch_contract_tc(g.sched, fp[0], fp[1], hi, lo, C, p->K, k0, k1,
+        launch_contract_tc(g.sched, fp[0], fp[1], split, C, C, p->K, k0, k1,
                            precision == BSK_PREC_BF16X3 ? 3 : 1, out, p->num_sms, st);
     }
   }
@@ -489,7 +483,7 @@ void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int prec
         seen[sl] = true;
         if (!p->slot[sl].fields) need += field_bytes;
       }
-    if (tc && !p->slot[c].hi) need += field_bytes;
+    if (tc && !p->slot[c].split) need += split_elems(p->n_alloc(), p->K) * sizeof(__nv_bfloat16);
     const int64_t held =
         p->stream_C ? (int64_t)p->stream_C * p->K * (12 + (p->stream_tc ? 4 : 0)) : 0;
     if (footprint(p) - held + (int64_t)need > (int64_t)p->mem_budget) {
@@ -504,14 +498,13 @@ void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int prec
   ensure_fields(p, a, st);
   ensure_fields(p, b, st);
   ensure_fields(p, c, st);
-  const __nv_bfloat16 *hi = nullptr, *lo = nullptr;
+  const __nv_bfloat16* split = nullptr;
   if (tc) {
     ensure_split(p, c, st);
-    hi = p->slot[c].hi;
-    lo = p->slot[c].lo;
+    split = p->slot[c].split;
   }
-  contract_dispatch(p, set, p->slot[a].fields, p->slot[b].fields, p->slot[c].fields, hi, lo,
-                    p->K, k0, k1, precision, out, st);
+  contract_dispatch(p, set, p->slot[a].fields, p->slot[b].fields, p->slot[c].fields, split,
+                    p->n_alloc(), p->K, k0, k1, precision, out, st);
   const double scale = std::pow(p->L, 6) / (double)p->K;
   launch_scale(out, set->T, scale, st);
 }
@@ -974,15 +967,13 @@ int bsk_contract(bsk_plan* p, const bsk_triset* set, const float* f1, const floa
     DeviceGuard g(p->device);
     cudaStream_t st = (cudaStream_t)stream;
     if (set->T == 0) return;
-    __nv_bfloat16 *hi = nullptr, *lo = nullptr;
+    __nv_bfloat16* split = nullptr;
     if (precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16) {
-      size_t n = (size_t)p->n * K;
-      hi = (__nv_bfloat16*)dmalloc_async(2 * n * sizeof(__nv_bfloat16), st);
-      lo = hi + n;
-      launch_split(f3, hi, lo, (int64_t)n, st);
+      split = (__nv_bfloat16*)dmalloc_async(split_elems(p->n, K) * sizeof(__nv_bfloat16), st);
+      launch_split(f3, p->n, K, split, st);
     }
-    contract_dispatch(p, set, f1, f2, f3, hi, lo, K, 0, K, precision, out, st);
-    if (hi) BSK_CHECK_CUDA(cudaFreeAsync(hi, st));
+    contract_dispatch(p, set, f1, f2, f3, split, p->n, K, 0, K, precision, out, st);
+    if (split) BSK_CHECK_CUDA(cudaFreeAsync(split, st));
   });
 }
 

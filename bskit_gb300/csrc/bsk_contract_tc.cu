@@ -6,8 +6,9 @@
 // columns, K slice of SLICE points), slice-major so that the CTAs running at
 // the same time share field data in L2.  Per 128-point pipeline stage:
 //   * warp 0 (one lane) TMA-loads into an SMEM ring (3 stages with one source
-//     tile, 2 with two) the bf16 hi and lo tiles of the column fields, per
-//     64-point K block as one 128-row operand (rows 0..63 hi, 64..127 lo;
+//     tile, 2 with two) the bf16 hi and lo tiles of the column fields in one copy
+//     from their chunk-major split ([block][plane][nc rows][64 points] per stage:
+//     per 64-point K block an operand of nc hi rows followed by nc lo rows;
 //     SWIZZLE_128B, K-major), and the FP32 tile(s) of the pair-factor shells
 //     (one tile when one range covers both factors of every row, as for auto
 //     spectra), each with only as many shell rows (16/32/48/64) as the tile uses.
@@ -91,13 +92,13 @@ constexpr int smem_bytes() {
   return Ring<kTwoSrc>::kStages * Ring<kTwoSrc>::kStageBytes + 1024 /*bars*/ + 1024 /*align*/;
 }
 
-// Tensor maps of one launch: bf16 column fields and FP32 sources, 16/32/64-row boxes
-// (2D, one 64- or 32-point block per copy), and the one-copy-per-stage views used
-// when the grid is a multiple of 128 points: B as {64 points, shell, hi/lo plane,
-// 64-point block} with box {64, nc, 2, 2}; sources as {32 points, shell, 32-point
-// block} with box {32, rows, 4}.
+// Tensor maps of one launch.  B: a 5D view of the chunk-major bf16 split {64 points,
+// shell, hi/lo plane, 64-point block, 128-point chunk} with box {64, nc, 2, 2, 1}: one
+// contiguous copy per stage.  Sources: FP32 [shell][K] with 16/32/64-row boxes (2D, one
+// 32-point block per copy) and, when the grid is a multiple of 128 points, the one-copy
+// view {32 points, shell, 32-point block} with box {32, rows, 4}.
 struct Maps {
-  CUtensorMap hi16, hi32, hi64, lo16, lo32, lo64, f1_16, f1_32, f1_64, f2_16, f2_32, f2_64;
+  CUtensorMap f1_16, f1_32, f1_64, f2_16, f2_32, f2_64;
   CUtensorMap b16, b32, b48, b64, a1_16, a1_32, a1_48, a1_64, a2_16, a2_32, a2_48, a2_64;
 };
 
@@ -193,6 +194,15 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map
       "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y, int z, int w, int v) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(v),
+      "r"(smem_u32(bar))
       : "memory");
 }
 __device__ __forceinline__ const CUtensorMap* by_rows(int n, const CUtensorMap* m16,
@@ -418,18 +428,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             break;
           }
           mbar_arrive_tx(&bars->full_b[s], b_bytes);
-          if (fused) {
-            // one copy for B (both 64-point blocks, hi and lo: [block][plane][nc rows])
-            tma_load_4d(st, by_rows(td.nc, &maps.b16, &maps.b32, &maps.b48, &maps.b64),
-                        &bars->full_b[s], 0, td.l0, 0, xi / KBLK);
-          } else {
-            for (int kb = 0; kb < KCH / KBLK; ++kb) {
-              load_rows(st + kb * B_BLOCK, &maps.hi16, &maps.hi32, &maps.hi64, &bars->full_b[s],
-                        xi + KBLK * kb, td.l0, td.nc);
-              load_rows(st + kb * B_BLOCK + B_TILE, &maps.lo16, &maps.lo32, &maps.lo64,
-                        &bars->full_b[s], xi + KBLK * kb, td.l0, td.nc);
-            }
-          }
+          // one contiguous copy for B: the stage's 128-point chunk of the split, nc shells,
+          // both planes, both 64-point blocks -> [block][plane][nc rows][64]
+          tma_load_5d(st, by_rows(td.nc, &maps.b16, &maps.b32, &maps.b48, &maps.b64),
+                      &bars->full_b[s], 0, td.l0, 0, 0, xi / KCH);
         }
       }
     }
@@ -445,11 +447,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       const TileDesc td = tiles[item % n_tiles];
       const int64_t x_begin = k_begin + sl * SLICE;
       const int64_t x_end = min(k_end, x_begin + SLICE);
-      // hi x [Bhi; Blo] (with 2D copies rows nc..63 of the hi block are not loaded:
-      // their accumulator columns are never read), lo x Bhi
-      // the lo rows of B sit right after the nc hi rows (one-copy loads) or 64 rows after
-      const int lo_row = fused ? td.nc : 64;
-      const uint32_t kb_bytes = fused ? 2u * td.nc * 128u : (uint32_t)B_BLOCK;
+      // hi x [Bhi; Blo] (the lo rows of a block sit right after its nc hi rows), lo x Bhi
+      const int lo_row = td.nc;
+      const uint32_t kb_bytes = 2u * td.nc * 128u;
       const uint32_t idesc_stack = idesc_bf16(terms >= 3 ? lo_row + td.nc : td.nc);
       const uint32_t idesc_hi = idesc_bf16(td.nc);
       for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
@@ -524,7 +524,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
             for (int e = 0; e < 16; ++e) acc[cc * 16 + e] += __uint_as_float(v[e]);
             if (terms >= 3) {
-              tmem_ld16(taddr + ACC_COL + b * 128 + (fused ? td.nc : 64) + cc * 16, v);
+              tmem_ld16(taddr + ACC_COL + b * 128 + td.nc + cc * 16, v);
 #pragma unroll
               for (int e = 0; e < 16; ++e) acc[cc * 16 + e] += __uint_as_float(v[e]);
             }
@@ -663,38 +663,41 @@ void make_map(CUtensorMap* m, CUtensorMapDataType dt, int esize, const void* bas
 }
 
 // View of a [rows][K] array with K cut into blocks of `blk` points:
-// dims {blk, rows, (planes,) K / blk}; box {blk, box_rows, (2,) nblk}.  Returns false
-// (map unusable) instead of failing when the driver rejects the layout.
+// dims {blk, rows, K / blk}; box {blk, box_rows, nblk}.  Returns false (map unusable)
+// instead of failing when the driver rejects the layout.
 bool make_block_map(CUtensorMap* m, CUtensorMapDataType dt, int esize, const void* base,
-                    int64_t K, int rows, int blk, int box_rows, int nblk, int64_t plane_bytes) {
-  const bool planes = plane_bytes > 0;
-  cuuint64_t dims[4], strides[3];
-  cuuint32_t box[4], estr[4] = {1, 1, 1, 1};
-  int rank;
-  if (planes) {
-    rank = 4;
-    dims[0] = (cuuint64_t)blk; dims[1] = (cuuint64_t)rows; dims[2] = 2;
-    dims[3] = (cuuint64_t)(K / blk);
-    strides[0] = (cuuint64_t)K * esize; strides[1] = (cuuint64_t)plane_bytes;
-    strides[2] = (cuuint64_t)blk * esize;
-    box[0] = blk; box[1] = box_rows; box[2] = 2; box[3] = nblk;
-  } else {
-    rank = 3;
-    dims[0] = (cuuint64_t)blk; dims[1] = (cuuint64_t)rows; dims[2] = (cuuint64_t)(K / blk);
-    strides[0] = (cuuint64_t)K * esize; strides[1] = (cuuint64_t)blk * esize;
-    box[0] = blk; box[1] = box_rows; box[2] = nblk;
-  }
-  CUresult r = encode_fn()(m, dt, rank, const_cast<void*>(base), dims, strides, box, estr,
+                    int64_t K, int rows, int blk, int box_rows, int nblk) {
+  cuuint64_t dims[3] = {(cuuint64_t)blk, (cuuint64_t)rows, (cuuint64_t)(K / blk)};
+  cuuint64_t strides[2] = {(cuuint64_t)K * esize, (cuuint64_t)blk * esize};
+  cuuint32_t box[3] = {(cuuint32_t)blk, (cuuint32_t)box_rows, (cuuint32_t)nblk};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = encode_fn()(m, dt, 3, const_cast<void*>(base), dims, strides, box, estr,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
 
+// The chunk-major bf16 split (split_index) as {64 points, shell, hi/lo plane, 64-point
+// block, 128-point chunk}; box {64, box_rows, 2, 2, 1} lands as [block][plane][rows][64].
+void make_split_map(CUtensorMap* m, const __nv_bfloat16* split, int S, int64_t K, int box_rows) {
+  cuuint64_t dims[5] = {64, (cuuint64_t)S, 2, 2, (cuuint64_t)((K + KCH - 1) / KCH)};
+  cuuint64_t strides[4] = {256, (cuuint64_t)S * 256, 128, (cuuint64_t)S * 512};
+  cuuint32_t box[5] = {64, (cuuint32_t)box_rows, 2, 2, 1};
+  cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  CUresult r = encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5,
+                           const_cast<__nv_bfloat16*>(split), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  BSK_REQUIRE(r == CUDA_SUCCESS, BSK_ERR_CUDA,
+              "cuTensorMapEncodeTiled (split) failed: " + std::to_string((int)r));
+}
+
 }  // namespace tc
 
 void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f2,
-                        const __nv_bfloat16* f3_hi, const __nv_bfloat16* f3_lo, int n_shells,
+                        const __nv_bfloat16* f3_split, int split_shells, int n_shells,
                         int64_t K, int64_t k_begin, int64_t k_end, int terms, double* out,
                         int num_sms, cudaStream_t st) {
   if (s.n_tiles == 0 || k_end <= k_begin) return;
@@ -704,13 +707,6 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
   BSK_REQUIRE(K < (int64_t)1 << 31, BSK_ERR_UNSUPPORTED, "grid too large for 32-bit TMA x");
   BSK_REQUIRE(K % 8 == 0, BSK_ERR_UNSUPPORTED, "K must be a multiple of 8");
   tc::Maps m;
-  const auto BF = CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-  tc::make_map(&m.hi16, BF, 2, f3_hi, K, n_shells, 64, 16);
-  tc::make_map(&m.hi32, BF, 2, f3_hi, K, n_shells, 64, 32);
-  tc::make_map(&m.hi64, BF, 2, f3_hi, K, n_shells, 64, 64);
-  tc::make_map(&m.lo16, BF, 2, f3_lo, K, n_shells, 64, 16);
-  tc::make_map(&m.lo32, BF, 2, f3_lo, K, n_shells, 64, 32);
-  tc::make_map(&m.lo64, BF, 2, f3_lo, K, n_shells, 64, 64);
   const auto F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
   tc::make_map(&m.f1_16, F32, 4, f1, K, n_shells, 32, 16);
   tc::make_map(&m.f1_32, F32, 4, f1, K, n_shells, 32, 32);
@@ -718,19 +714,16 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
   tc::make_map(&m.f2_16, F32, 4, f2, K, n_shells, 32, 16);
   tc::make_map(&m.f2_32, F32, 4, f2, K, n_shells, 32, 32);
   tc::make_map(&m.f2_64, F32, 4, f2, K, n_shells, 32, 64);
-  // One copy per stage for B and per source tile when K is a multiple of the stage and
-  // hi / lo are two planes of one allocation (lo above hi, 16-byte multiple apart).
-  const int64_t plane = (int64_t)((const char*)f3_lo - (const char*)f3_hi);
-  bool fused = K % tc::KCH == 0 && plane > 0 && plane % 16 == 0;
   const int rows16[4] = {16, 32, 48, 64};
   CUtensorMap* bmaps[4] = {&m.b16, &m.b32, &m.b48, &m.b64};
   CUtensorMap* a1maps[4] = {&m.a1_16, &m.a1_32, &m.a1_48, &m.a1_64};
   CUtensorMap* a2maps[4] = {&m.a2_16, &m.a2_32, &m.a2_48, &m.a2_64};
+  for (int i = 0; i < 4; ++i) tc::make_split_map(bmaps[i], f3_split, split_shells, K, rows16[i]);
+  // one copy per stage per source tile when K is a multiple of the stage
+  bool fused = K % tc::KCH == 0;
   for (int i = 0; i < 4 && fused; ++i) {
-    fused = tc::make_block_map(bmaps[i], BF, 2, f3_hi, K, n_shells, tc::KBLK, rows16[i],
-                               tc::KCH / tc::KBLK, plane) &&
-            tc::make_block_map(a1maps[i], F32, 4, f1, K, n_shells, 32, rows16[i], 4, 0) &&
-            tc::make_block_map(a2maps[i], F32, 4, f2, K, n_shells, 32, rows16[i], 4, 0);
+    fused = tc::make_block_map(a1maps[i], F32, 4, f1, K, n_shells, 32, rows16[i], 4) &&
+            tc::make_block_map(a2maps[i], F32, 4, f2, K, n_shells, 32, rows16[i], 4);
   }
   bool two_src = f1 != f2;
   for (const TileDesc& d : s.h_tiles) two_src = two_src || d.i0 != d.j0;

@@ -97,12 +97,21 @@ struct StreamBuf {
 };
 
 // ---------------------------------------------------------------- plan
+// The bf16 hi / lo split of S shell fields over K points is stored chunk-major:
+// [ceil(K / 128) chunks][hi, lo][S shells][128 points], so that the column tiles of one
+// 128-point contraction stage (nc shells, both planes) are one contiguous block for TMA
+// (256-byte pieces of rows a plane apart were ~20% slower to stream).  The tail of the last
+// chunk (points K .. 128 ceil(K / 128)) is zero.
+inline size_t split_elems(int S, int64_t K) { return (size_t)((K + 127) / 128) * 256 * S; }
+__host__ __device__ __forceinline__ int64_t split_index(int plane, int s, int64_t x, int S) {
+  return (x >> 7) * (256 * (int64_t)S) + ((int64_t)plane * S + s) * 128 + (x & 127);
+}
+
 struct FieldSlot {
   bool painted = false;
   cufftComplex* spec = nullptr;   // coarse half spectrum, scaled 1/N^3 (Ng*Ng*(Ng/2+1))
   float* fields = nullptr;        // [n][K] FP32 shell fields (nullptr until built)
-  __nv_bfloat16* hi = nullptr;    // [n][K] bf16 split (nullptr until built)
-  __nv_bfloat16* lo = nullptr;
+  __nv_bfloat16* split = nullptr; // bf16 split of the n_alloc shells, chunk-major (above)
   bool fields_ok = false;
   bool split_ok = false;
   int64_t gen = 0;                // bumped by every paint (keys of streamed fields)
@@ -195,11 +204,11 @@ size_t synth_workspace_bytes(int n, int max_r, int batch);
 // Twiddle table at the start of the workspace (synchronous; once, after allocation).
 void synth_init_workspace(int n, void* work);
 void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0, int ns, int R,
-                  void* work, float* fields, __nv_bfloat16* hi, __nv_bfloat16* lo,
+                  void* work, float* fields, __nv_bfloat16* split, int split_shells,
                   cudaStream_t st, int out_s0 = 0);
-// FP32 -> (bf16 hi, bf16 lo) split, n elements.
-void launch_split(const float* in, __nv_bfloat16* hi, __nv_bfloat16* lo, int64_t n,
-                  cudaStream_t st);
+// FP32 fields [S][K] -> their chunk-major bf16 hi / lo split (split_elems(S, K) values,
+// the tail of the last chunk zeroed).
+void launch_split(const float* in, int S, int64_t K, __nv_bfloat16* split, cudaStream_t st);
 
 // SIMT contraction (Tin = float|double input fields, Tacc = float|double tile sums).
 // out[t] += sum over K of f1[i] f2[j] f3[l]  (out must be zeroed by the caller).
@@ -215,7 +224,7 @@ void launch_contract_simt_d64(const DeviceSchedule& s, const double* f1, const d
 
 // tcgen05 contraction: f1/f2 FP32 (pair-product sources), f3 as bf16 hi/lo.
 void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f2,
-                        const __nv_bfloat16* f3_hi, const __nv_bfloat16* f3_lo, int n_shells,
+                        const __nv_bfloat16* f3_split, int split_shells, int n_shells,
                         int64_t K, int64_t k_begin, int64_t k_end, int terms, double* out,
                         int num_sms, cudaStream_t st);
 

@@ -156,12 +156,12 @@ extern "C" int bsk_contract_noalloc(int n_shells, int64_t n_tri, const int32_t* 
     const size_t b_tiles = align256(tb.tiles.size() * sizeof(TileDesc));
     const size_t b_rows = align256(tb.ri.size() * sizeof(int16_t));
     const size_t b_map = align256(tb.map.size() * sizeof(int32_t));
-    const size_t b_split = align256((size_t)n_shells * k_points * sizeof(__nv_bfloat16));
-    const size_t need = b_tiles + 2 * b_rows + b_map + 2 * b_split;
+    const size_t b_split = align256(split_elems(n_shells, k_points) * sizeof(__nv_bfloat16));
+    const size_t need = b_tiles + 2 * b_rows + b_map + b_split;
     BSK_REQUIRE(need <= kStaticScratchBytes, BSK_ERR_ARG,
                 "request needs " + std::to_string(need) + " bytes of scratch; the static area "
                 "holds " + std::to_string(kStaticScratchBytes) + " (n_shells * k_points * 4 "
-                "bytes plus the schedule)");
+                "bytes, k_points rounded up to a multiple of 128, plus the schedule)");
 
     unsigned char* base = (unsigned char*)scratch_address(dev);
     DeviceSchedule s;
@@ -171,9 +171,8 @@ extern "C" int bsk_contract_noalloc(int n_shells, int64_t n_tri, const int32_t* 
     s.row_j = reinterpret_cast<int16_t*>(base + b_tiles + b_rows);
     s.map = reinterpret_cast<int32_t*>(base + b_tiles + 2 * b_rows);
     s.h_tiles = tb.tiles;
-    __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(base + b_tiles + 2 * b_rows + b_map);
-    __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(base + b_tiles + 2 * b_rows + b_map +
-                                                          b_split);
+    __nv_bfloat16* split =
+        reinterpret_cast<__nv_bfloat16*>(base + b_tiles + 2 * b_rows + b_map);
     BSK_CHECK_CUDA(cudaMemcpyAsync(s.tiles, tb.tiles.data(), tb.tiles.size() * sizeof(TileDesc),
                                    cudaMemcpyHostToDevice, st));
     BSK_CHECK_CUDA(cudaMemcpyAsync(s.row_i, tb.ri.data(), tb.ri.size() * sizeof(int16_t),
@@ -184,9 +183,9 @@ extern "C" int bsk_contract_noalloc(int n_shells, int64_t n_tri, const int32_t* 
                                    cudaMemcpyHostToDevice, st));
     // host vectors are released at return: the copies above must have read them
     BSK_CHECK_CUDA(cudaStreamSynchronize(st));
-    launch_split(f3, hi, lo, (int64_t)n_shells * k_points, st);
+    launch_split(f3, n_shells, k_points, split, st);  // also zeroes the last chunk's tail
     BSK_CHECK_CUDA(cudaMemsetAsync(out, 0, (size_t)n_tri * sizeof(double), st));
-    launch_contract_tc(s, f1, f2, hi, lo, n_shells, k_points, 0, k_points,
+    launch_contract_tc(s, f1, f2, split, n_shells, n_shells, k_points, 0, k_points,
                        precision == BSK_PREC_BF16X3 ? 3 : 1, out, num_sms, st);
     s.tiles = nullptr;  // the schedule lives in the static area: nothing to release
     s.row_i = s.row_j = nullptr;

@@ -178,23 +178,29 @@ __global__ void filter_indicator_kernel(int Ng, double kf, const uint16_t* __res
   }
 }
 
-__global__ void split_kernel(const float4* __restrict__ in, uint2* __restrict__ hi,
-                             uint2* __restrict__ lo, int64_t n4) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4;
+// FP32 fields [S][K] -> their chunk-major bf16 hi / lo split (split_index), hi = bf16_rn(v),
+// lo = bf16_rn(v - hi); 4 points per thread (K % 4 == 0, so a quad never straddles a
+// 128-point chunk); the points K .. 128 ceil(K / 128) of the last chunk are written as zeros.
+__global__ void split_kernel(const float4* __restrict__ in, __nv_bfloat16* __restrict__ split,
+                             int S, int64_t K, int64_t quads_per_shell) {
+  const int64_t n = (int64_t)S * quads_per_shell;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    float4 v = __ldg(in + i);
-    __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y);
-    __nv_bfloat162 h23 = __floats2bfloat162_rn(v.z, v.w);
-    float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
-    __nv_bfloat162 l01 = __floats2bfloat162_rn(v.x - f01.x, v.y - f01.y);
-    __nv_bfloat162 l23 = __floats2bfloat162_rn(v.z - f23.x, v.w - f23.y);
-    uint2 H, Lo;
-    H.x = *reinterpret_cast<uint32_t*>(&h01);
-    H.y = *reinterpret_cast<uint32_t*>(&h23);
-    Lo.x = *reinterpret_cast<uint32_t*>(&l01);
-    Lo.y = *reinterpret_cast<uint32_t*>(&l23);
-    hi[i] = H;
-    lo[i] = Lo;
+    const int s = (int)(i / quads_per_shell);
+    const int64_t x = (i - (int64_t)s * quads_per_shell) * 4;
+    const float4 v = x < K ? __ldg(in + ((int64_t)s * K + x) / 4) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y);
+    const __nv_bfloat162 h23 = __floats2bfloat162_rn(v.z, v.w);
+    const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
+    const __nv_bfloat162 l01 = __floats2bfloat162_rn(v.x - f01.x, v.y - f01.y);
+    const __nv_bfloat162 l23 = __floats2bfloat162_rn(v.z - f23.x, v.w - f23.y);
+    uint2 hv, lv;
+    hv.x = *reinterpret_cast<const uint32_t*>(&h01);
+    hv.y = *reinterpret_cast<const uint32_t*>(&h23);
+    lv.x = *reinterpret_cast<const uint32_t*>(&l01);
+    lv.y = *reinterpret_cast<const uint32_t*>(&l23);
+    *reinterpret_cast<uint2*>(split + split_index(0, s, x, S)) = hv;
+    *reinterpret_cast<uint2*>(split + split_index(1, s, x, S)) = lv;
   }
 }
 
@@ -275,12 +281,12 @@ void launch_filter_indicator(const bsk_plan* p, int s0, int ns, int kweight,
   BSK_CHECK_CUDA(cudaGetLastError());
 }
 
-void launch_split(const float* in, __nv_bfloat16* hi, __nv_bfloat16* lo, int64_t n,
-                  cudaStream_t st) {
-  int64_t n4 = n / 4;  // n is a multiple of 4 (Ng even => Ng^3 % 8 == 0)
-  split_kernel<<<grid_for(n4, 256, 152 * 16), 256, 0, st>>>(
-      reinterpret_cast<const float4*>(in), reinterpret_cast<uint2*>(hi),
-      reinterpret_cast<uint2*>(lo), n4);
+void launch_split(const float* in, int S, int64_t K, __nv_bfloat16* split, cudaStream_t st) {
+  BSK_REQUIRE(K % 4 == 0, BSK_ERR_UNSUPPORTED, "the bf16 split wants a multiple of 4 points");
+  if (S <= 0 || K <= 0) return;
+  const int64_t quads = (K + 127) / 128 * 32;
+  split_kernel<<<grid_for((int64_t)S * quads, 256, 152 * 16), 256, 0, st>>>(
+      reinterpret_cast<const float4*>(in), split, S, K, quads);
   BSK_CHECK_CUDA(cudaGetLastError());
 }
 

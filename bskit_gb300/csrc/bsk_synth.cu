@@ -305,8 +305,8 @@ struct SynthArgs {
   float2* G;               // [s][x][bk][c]   (c < Cp)
   float2* Hh;              // [s][x][y][c]
   float* fields;           // [shell][N^3], shell index s0 + s
-  __nv_bfloat16* hi;       // optional [shell][N^3]
-  __nv_bfloat16* lo;
+  __nv_bfloat16* split;    // optional chunk-major hi / lo split of split_shells shells
+  int split_shells;
   const float2* tw;        // [N] e^{+2 pi i k / N}
 };
 
@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(kThreads, 2) synth_y_kernel(SynthArgs A, FftPl
 template <int NC>
 __device__ __forceinline__ void z_last_pass(const float2* __restrict__ src,
                                             const float2* __restrict__ tw, const FftPlan& pl,
-                                            const SynthArgs& A, int64_t base, int y0) {
+                                            const SynthArgs& A, int sh, int64_t row0, int y0) {
   constexpr int np = plan_np(NC);
   constexpr int R = plan_radix(NC, np - 1);
   constexpr int M = NC / R;
@@ -458,20 +458,21 @@ __device__ __forceinline__ void z_last_pass(const float2* __restrict__ src,
     dft_radix<R>(v, pl);
     const bool odd = j & 1;
     const int y = y0 + 2 * line + (odd ? 1 : 0);
-    const int64_t o = base + (int64_t)y * NC + (j & ~1);
+    const int64_t K = (int64_t)NC * NC * NC;
+    const int64_t o = row0 + (int64_t)y * NC + (j & ~1);  // point index within the shell
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const float got = __shfl_xor_sync(0xffffffffu, odd ? v[r].x : v[r].y, 1);
       const float2 f = odd ? make_float2(got, v[r].y) : make_float2(v[r].x, got);
       if (y < NC) {
-        const int64_t p = o + (int64_t)M * r;
-        *reinterpret_cast<float2*>(A.fields + p) = f;
-        if (A.hi) {
+        const int64_t pt = o + (int64_t)M * r;
+        *reinterpret_cast<float2*>(A.fields + (int64_t)sh * K + pt) = f;
+        if (A.split) {
           const __nv_bfloat162 h = __floats2bfloat162_rn(f.x, f.y);
           const float2 fb = __bfloat1622float2(h);
           const __nv_bfloat162 lw = __floats2bfloat162_rn(f.x - fb.x, f.y - fb.y);
-          *reinterpret_cast<__nv_bfloat162*>(A.hi + p) = h;
-          *reinterpret_cast<__nv_bfloat162*>(A.lo + p) = lw;
+          *reinterpret_cast<__nv_bfloat162*>(A.split + split_index(0, sh, pt, A.split_shells)) = h;
+          *reinterpret_cast<__nv_bfloat162*>(A.split + split_index(1, sh, pt, A.split_shells)) = lw;
         }
       }
     }
@@ -538,12 +539,13 @@ __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPl
     __syncthreads();
     if (u + (int)gridDim.x < units) fetch(u + gridDim.x);
     const int64_t K = (int64_t)N * N * N;
-    const int64_t base = (int64_t)(A.s0 + s - A.out0) * K + ((int64_t)x * N) * N;
+    const int sh = A.s0 + s - A.out0;  // shell index in the output arrays
+    const int64_t row0 = ((int64_t)x * N) * N;
     if constexpr (NC != 0) {
       float2* src = buf0;
       float2* dst = buf1;
       run_passes_but_last<NC, kZLines, 0, 1>(src, dst, tw, pl);
-      z_last_pass<NC>(src, tw, pl, A, base, y0);
+      z_last_pass<NC>(src, tw, pl, A, sh, row0, y0);
     } else {
       const float2* res = fft_lines<NC, kZLines>(buf0, buf1, pl, tw);
       // four consecutive z per thread: 16-byte field stores, 8-byte hi / lo stores (N % 4 == 0)
@@ -556,9 +558,9 @@ __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPl
         float4 v;
         if (rr & 1) v = make_float4(w[0].y, w[1].y, w[2].y, w[3].y);
         else v = make_float4(w[0].x, w[1].x, w[2].x, w[3].x);
-        const int64_t o = base + (int64_t)y * N + z;
-        *reinterpret_cast<float4*>(A.fields + o) = v;
-        if (A.hi) {
+        const int64_t pt = row0 + (int64_t)y * N + z;
+        *reinterpret_cast<float4*>(A.fields + (int64_t)sh * K + pt) = v;
+        if (A.split) {
           const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y);
           const __nv_bfloat162 h23 = __floats2bfloat162_rn(v.z, v.w);
           const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
@@ -569,8 +571,8 @@ __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPl
           hv.y = *reinterpret_cast<const uint32_t*>(&h23);
           lv.x = *reinterpret_cast<const uint32_t*>(&l01);
           lv.y = *reinterpret_cast<const uint32_t*>(&l23);
-          *reinterpret_cast<uint2*>(A.hi + o) = hv;
-          *reinterpret_cast<uint2*>(A.lo + o) = lv;
+          *reinterpret_cast<uint2*>(A.split + split_index(0, sh, pt, A.split_shells)) = hv;
+          *reinterpret_cast<uint2*>(A.split + split_index(1, sh, pt, A.split_shells)) = lv;
         }
       }
     }
@@ -656,7 +658,7 @@ void synth_init_workspace(int N, void* work) {
 }
 
 void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0, int ns, int R,
-                  void* work, float* fields, __nv_bfloat16* hi, __nv_bfloat16* lo,
+                  void* work, float* fields, __nv_bfloat16* split, int split_shells,
                   cudaStream_t st, int out_s0) {
   FftPlan pl;
   BSK_REQUIRE(make_plan(N, pl), BSK_ERR_UNSUPPORTED, "no FFT plan for this grid size");
@@ -678,8 +680,8 @@ void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0
   A.G = tw + N;
   A.Hh = A.G + (size_t)ns * N * nk * Cp;
   A.fields = fields;
-  A.hi = hi;
-  A.lo = lo;
+  A.split = split;
+  A.split_shells = split_shells;
   A.tw = tw;
   const size_t fft_smem = (2 * (size_t)kLines * (N + 1) + N) * sizeof(float2);
   const size_t x_smem = (2 * (size_t)kXLines * (N + 1) + N) * sizeof(float2) +

@@ -127,6 +127,19 @@ def test_fields_match_oracle_native(cuda, n):
         assert np.abs(f - of[s]).max() <= 1e-5 * scale, s
 
 
+def test_fields_match_oracle_native_192(cuda):
+    # the compile-time 16 x 12 plan (the 256^3 workload's contraction grid), 5 shells
+    n, box, edges, _ = _small(192, 100.0, 8, 0.25)
+    delta = synthetic.lognormal_mesh(n, box, seed=13)
+    plan = Plan(n, box, edges, grid="native")
+    plan.paint(0, torch.from_numpy(delta))
+    of = O.shell_fields(O.spectrum(delta), n, box, edges)
+    for s in range(len(edges)):
+        f = plan.field(0, s).cpu().numpy().astype(np.float64)
+        scale = np.abs(of[s]).max()
+        assert np.abs(f - of[s]).max() <= 1e-5 * scale, s
+
+
 def test_paint_keeps_input(cuda):
     n, box, edges, _ = _small(32, 100.0, 2)
     delta = torch.from_numpy(synthetic.lognormal_mesh(n, box, seed=12)).cuda()
@@ -164,6 +177,28 @@ def test_auto_bispectrum_more_shells(cuda, prec):
     of = O.shell_fields(O.spectrum(delta), n, box, edges)
     bo = O.triple_sums(of, of, of, tri) * box ** 6 / n ** 3
     _check_b(b.cpu().numpy(), bo, _abs_sums(of, of, of, tri, box, n), prec)
+
+
+def test_contract_ragged_grid_matches_fp64(cuda):
+    # K = 36^3 = 46656 is not a multiple of 128: the tensor-core path loads the sources with
+    # per-quarter copies and the column operand from a split whose last chunk is half padding
+    kf = TWO_PI / 100.0
+    kw = dict(kmin=kf, kmax=16 * kf, dk=2 * kf)
+    edges = B.generate_bin_edge_list(**kw)
+    tri = B.generate_triangle_bin_list(return_indices=True, **kw)
+    n, K = len(edges), 36 ** 3
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    fs = [torch.randn((n, K), generator=g, device="cuda") for _ in range(3)]
+    plan = Plan(64, 100.0, edges)
+    ts = plan.triangles(tri)
+    b64 = plan.contract(ts, *fs, precision="fp64").cpu().numpy()
+    babs = plan.contract(ts, *[f.abs() for f in fs], precision="fp64").cpu().numpy()
+    for prec, bound in (("bf16x3", 4e-6), ("bf16", 1e-3)):
+        b = plan.contract(ts, *fs, precision=prec).cpu().numpy()
+        assert np.all(np.isfinite(b))
+        assert (np.abs(b - b64) / babs).max() <= bound, prec
+    plan.sync_check()
 
 
 @pytest.mark.parametrize("prec", ["fp64", "bf16x3"])
