@@ -16,7 +16,8 @@
 //     them and its B tiles once the stage's MMAs completed, each part with its own
 //     "landed" barrier, so the sources get about one more stage of lead time;
 //   * warps 10..17 (2 per TMEM lane quadrant, one 64-point half each) read the
-//     row's F1_i, F2_j from SMEM, form P = F1_i*F2_j with packed f32x2
+//     row's F1_i, F2_j from SMEM (one 8-point group ahead of the math), form
+//     P = F1_i*F2_j with packed f32x2
 //     arithmetic, split P = hi + lo (bf16 round-to-nearest) and store them with
 //     tcgen05.st into the 2-stage TMEM A-operand ring (lane = GEMM row);
 //   * warp 1 runs the stage loop and one elected lane issues, per 16-point K step,
@@ -44,11 +45,11 @@ namespace bsk {
 namespace tc {
 
 constexpr int KCH = 128;                      // points per pipeline stage
-constexpr int KBLK = 64;                      // points per SWIZZLE_128B K block of the B operand
 constexpr int ACC_CHUNKS = 1;                 // stages summed inside one TMEM accumulator
 constexpr int ASTAGES = 2;                    // TMEM A-operand ring
 constexpr int NACC = 2;                       // TMEM accumulators
-constexpr int B_TILE = kMaxCols * 128;        // 8 KB: 64 rows x 64 bf16 (one K block, hi or lo)
+constexpr int B_TILE = kMaxCols * 128;        // 8 KB: 64 rows x 64 bf16 (one 64-point SWIZZLE_128B
+                                              // K block of the B operand, hi or lo)
 constexpr int B_BLOCK = 2 * B_TILE;           // 16 KB: hi then lo of one K block
 constexpr int A_QUARTER = kMaxSrcRows * 128;  // 8 KB: 64 rows x 32 fp32
 constexpr int A_TILE = 4 * A_QUARTER;         // 32 KB: one source tile of a stage
@@ -582,30 +583,48 @@ __global__ void __launch_bounds__(THREADS, 1)
         tc_fence_after();
         const uint8_t* st = smem + s * STAGE_BYTES;
         const uint32_t a_hi = tmem + tlane + A_COL + a * 128 + half * 32;
-#pragma unroll
-        for (int sub = 0; sub < 4; ++sub) {
-          // points 64 half + 16 sub .. +16: quarter 2 half + sub / 2 of the source tile
+        // The warp's 64 points in 8 groups of 8; the shared-memory loads of group g + 1 are
+        // issued before the math of group g (software pipelining: the loads' latency, not
+        // the load pipe's bandwidth, bounds these warps).  Group g covers the 16-byte chunks
+        // c = 4 (sub & 1) + 2 (g & 1) + e (e < 2) of quarter 2 half + sub / 2 of the source
+        // tile, sub = g / 2; two groups fill one 16-point K step of the A operand.
+        auto load_group = [&](int g, ulonglong2 (&va)[2], ulonglong2 (&vb)[2]) {
+          const int sub = g >> 1;
           const int qq = 2 * half + (sub >> 1);
           const uint8_t* row1 = st + 2 * B_BLOCK + qq * qstride + pi * 128;
           const uint8_t* row2 = st + 2 * B_BLOCK + src2 + qq * qstride2 + pj * 128;
-          uint32_t hi[8], lo[8];
-          if (valid) {
 #pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4) {
-              const int c = (sub & 1) * 4 + c4;  // logical 16-B chunk (4 floats) of the row
-              const ulonglong2 va =
-                  *reinterpret_cast<const ulonglong2*>(row1 + ((c ^ (pi & 7)) << 4));
-              const ulonglong2 vb =
-                  *reinterpret_cast<const ulonglong2*>(row2 + ((c ^ (pj & 7)) << 4));
-              split2(f2_mul(va.x, vb.x), hi[2 * c4], lo[2 * c4]);
-              split2(f2_mul(va.y, vb.y), hi[2 * c4 + 1], lo[2 * c4 + 1]);
-            }
-          } else {
-#pragma unroll
-            for (int e = 0; e < 8; ++e) hi[e] = lo[e] = 0u;
+          for (int e = 0; e < 2; ++e) {
+            const int c = (sub & 1) * 4 + (g & 1) * 2 + e;
+            va[e] = *reinterpret_cast<const ulonglong2*>(row1 + ((c ^ (pi & 7)) << 4));
+            vb[e] = *reinterpret_cast<const ulonglong2*>(row2 + ((c ^ (pj & 7)) << 4));
           }
-          tmem_st8(a_hi + sub * 8, hi);
-          tmem_st8(a_hi + 64 + sub * 8, lo);
+        };
+        ulonglong2 ca[2], cb[2], na[2], nb[2];
+        load_group(0, ca, cb);
+        uint32_t hi[8], lo[8];
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+          if (g + 1 < 8) load_group(g + 1, na, nb);
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const int c4 = (g & 1) * 2 + e;
+            split2(f2_mul(ca[e].x, cb[e].x), hi[2 * c4], lo[2 * c4]);
+            split2(f2_mul(ca[e].y, cb[e].y), hi[2 * c4 + 1], lo[2 * c4 + 1]);
+          }
+          if (g & 1) {
+            if (!valid) {  // rows past the tile's pairs: zeros (their sums are never read)
+#pragma unroll
+              for (int e = 0; e < 8; ++e) hi[e] = lo[e] = 0u;
+            }
+            tmem_st8(a_hi + (g >> 1) * 8, hi);
+            tmem_st8(a_hi + 64 + (g >> 1) * 8, lo);
+          }
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            ca[e] = na[e];
+            cb[e] = nb[e];
+          }
         }
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         tc_fence_before();
