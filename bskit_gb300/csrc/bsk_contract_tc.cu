@@ -3,7 +3,7 @@
 //   C[(i,j), l] += sum_x P_ij(x) * F3_l(x),   P_ij = F1_i * F2_j  (FP32, formed on chip)
 //
 // One persistent CTA per SM walks work items (tile of 128 pair rows x nc <= 64
-// columns, K slice of SLICE points), slice-major so that the CTAs running at
+// columns, K slice of `slice` points), slice-major so that the CTAs running at
 // the same time share field data in L2.  Per 128-point pipeline stage:
 //   * warp 0 (one lane) TMA-loads into an SMEM ring (3 stages with one source
 //     tile, 2 with two) the bf16 hi and lo tiles of the column fields in one copy
@@ -58,7 +58,12 @@ constexpr int THREADS = NUM_WARPS * 32;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_COL = 0;               // accumulator b at 128 b: [0,64) hi*B+lo*Bhi, [64,128) hi*Blo
 constexpr uint32_t A_COL = 256;               // A stage a at 256 + 128 a: hi +0..63, lo +64..127
-constexpr int64_t SLICE = 16384;              // points per work item
+// Points per work item: 32 768 when that still gives every SM at least kMinItemsPerSm
+// items (one CTA per SM walks them), else 16 384.  Longer slices spread the per-item
+// epilogue (the FP64 atomics of the tile's bins) over more stages: 24.2 -> 23.1 ms on the
+// 512^3 headline; shorter ones keep small problems spread over all SMs.
+constexpr int64_t kSliceLong = 32768, kSliceShort = 16384;
+constexpr int64_t kMinItemsPerSm = 8;
 constexpr unsigned long long kTimeoutNs = 2000000000ull;
 
 // An SMEM stage holds two K blocks of B hi / lo (32 KB) + one or two FP32 source
@@ -325,13 +330,14 @@ __device__ __forceinline__ void split2(unsigned long long p, uint32_t& hi, uint3
 }
 
 // 18 warps: 5 share one SM sub-partition, whose 16K registers allow 102 per thread.
-template <bool kTwoSrc>
+template <bool kTwoSrc, bool kLongSlice>
 __global__ void __launch_bounds__(THREADS, 1)
     contract_tc_kernel(const __grid_constant__ Maps maps, const TileDesc* __restrict__ tiles,
                        const int16_t* __restrict__ row_i, const int16_t* __restrict__ row_j,
                        const int32_t* __restrict__ map, int n_tiles, int same_src,
                        int64_t k_begin, int64_t k_end, int64_t n_items, int terms, int fused,
                        double* __restrict__ out) {
+  constexpr int64_t slice = kLongSlice ? kSliceLong : kSliceShort;
   constexpr int STAGE_BYTES = Ring<kTwoSrc>::kStageBytes;
   constexpr int SST = Ring<kTwoSrc>::kStages;
   extern __shared__ uint8_t smem_raw[];
@@ -385,8 +391,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int64_t sl = item / n_tiles;
         const TileDesc td = tiles[item % n_tiles];
         const bool one_src = !kTwoSrc || (same_src && td.i0 == td.j0);
-        const int64_t x_begin = k_begin + sl * SLICE;
-        const int64_t x_end = min(k_end, x_begin + SLICE);
+        const int64_t x_begin = k_begin + sl * slice;
+        const int64_t x_end = min(k_end, x_begin + slice);
         // bytes per stage: the four 32-point quarters of each source tile; the column rows
         // of hi and lo in both K blocks
         const uint32_t src_bytes =
@@ -446,8 +452,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int64_t item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
       const int64_t sl = item / n_tiles;
       const TileDesc td = tiles[item % n_tiles];
-      const int64_t x_begin = k_begin + sl * SLICE;
-      const int64_t x_end = min(k_end, x_begin + SLICE);
+      const int64_t x_begin = k_begin + sl * slice;
+      const int64_t x_end = min(k_end, x_begin + slice);
       // hi x [Bhi; Blo] (the lo rows of a block sit right after its nc hi rows), lo x Bhi
       const int lo_row = td.nc;
       const uint32_t kb_bytes = 2u * td.nc * 128u;
@@ -502,8 +508,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int64_t item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
       const int64_t sl = item / n_tiles;
       const TileDesc td = tiles[item % n_tiles];
-      const int64_t x_begin = k_begin + sl * SLICE;
-      const int64_t x_end = min(k_end, x_begin + SLICE);
+      const int64_t x_begin = k_begin + sl * slice;
+      const int64_t x_end = min(k_end, x_begin + slice);
       const int64_t nch = (x_end - x_begin + KCH - 1) / KCH;
       const int64_t ngrp = (nch + ACC_CHUNKS - 1) / ACC_CHUNKS;
       float acc[32];
@@ -557,8 +563,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int64_t sl = item / n_tiles;
       const TileDesc td = tiles[item % n_tiles];
       const bool one_src = !kTwoSrc || (same_src && td.i0 == td.j0);
-      const int64_t x_begin = k_begin + sl * SLICE;
-      const int64_t x_end = min(k_end, x_begin + SLICE);
+      const int64_t x_begin = k_begin + sl * slice;
+      const int64_t x_end = min(k_end, x_begin + slice);
       const int ri = row_i[td.row_off + r];
       const int rj = row_j[td.row_off + r];
       const bool valid = ri >= 0;
@@ -746,19 +752,26 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
   }
   bool two_src = f1 != f2;
   for (const TileDesc& d : s.h_tiles) two_src = two_src || d.i0 != d.j0;
+  const bool long_slice = (k_end - k_begin + tc::kSliceLong - 1) / tc::kSliceLong * s.n_tiles >=
+                         tc::kMinItemsPerSm * num_sms;
+  const int64_t slice = long_slice ? tc::kSliceLong : tc::kSliceShort;
+  const int64_t n_slices = (k_end - k_begin + slice - 1) / slice;
+  const int64_t n_items = n_slices * s.n_tiles;
   constexpr int kMaxDev = 64;
-  static bool attr_set[kMaxDev][2] = {};
+  static bool attr_set[kMaxDev][4] = {};
   int dev = 0;
   BSK_CHECK_CUDA(cudaGetDevice(&dev));
   BSK_REQUIRE(dev < kMaxDev, BSK_ERR_UNSUPPORTED, "device ordinal above 63");
-  auto kern = two_src ? tc::contract_tc_kernel<true> : tc::contract_tc_kernel<false>;
+  auto kern = two_src ? (long_slice ? tc::contract_tc_kernel<true, true>
+                                    : tc::contract_tc_kernel<true, false>)
+                      : (long_slice ? tc::contract_tc_kernel<false, true>
+                                    : tc::contract_tc_kernel<false, false>);
   const int smem = two_src ? tc::smem_bytes<true>() : tc::smem_bytes<false>();
-  if (!attr_set[dev][two_src]) {
+  const int variant = (two_src ? 2 : 0) + (long_slice ? 1 : 0);
+  if (!attr_set[dev][variant]) {
     BSK_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    attr_set[dev][two_src] = true;
+    attr_set[dev][variant] = true;
   }
-  const int64_t n_slices = (k_end - k_begin + tc::SLICE - 1) / tc::SLICE;
-  const int64_t n_items = n_slices * s.n_tiles;
   int64_t grid = num_sms;
   if (grid > n_items) grid = n_items;
   kern<<<(unsigned)grid, tc::THREADS, smem, st>>>(
