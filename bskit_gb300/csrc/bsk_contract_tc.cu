@@ -17,13 +17,13 @@
 //     "landed" barrier, so the sources get about one more stage of lead time;
 //   * warps 10..17 (2 per TMEM lane quadrant, one 64-point half each) read the
 //     row's F1_i, F2_j from SMEM (one 8-point group ahead of the math), form
-//     P = F1_i*F2_j with packed f32x2
-//     arithmetic, split P = hi + lo (bf16 round-to-nearest) and store them with
-//     tcgen05.st into the 2-stage TMEM A-operand ring (lane = GEMM row);
+//     P = F1_i*F2_j with packed f32x2 arithmetic, split P = hi + lo (bf16
+//     round-to-nearest) and store them with tcgen05.st into the 2-stage TMEM
+//     A-operand ring (lane = GEMM row);
 //   * warp 1 runs the stage loop and one elected lane issues, per 16-point K step,
 //     tcgen05.mma kind::f16 with A from TMEM and B from SMEM: hi x [Bhi; Blo]
-//     (N = 2 nc, or 64 + nc with 2D copies: one MMA yields both hi*Bhi and hi*Blo)
-//     and, for bf16x3, lo x Bhi (N = nc).  The tensor core's FP32 accumulate
+//     (N = 2 nc: one MMA yields both hi*Bhi and hi*Blo) and, for bf16x3, lo x Bhi
+//     (N = nc, into the hi*Bhi columns).  The tensor core's FP32 accumulate
 //     truncates, so an accumulator is only ever fed one stage (16 MMAs) before it is
 //     handed over;
 //   * warps 2..9 (2 per lane quadrant, 32 columns each) drain each finished
@@ -33,8 +33,8 @@
 //     (atomics).
 // The MMAs' completion is committed once per stage, to a ring of mbarriers that
 // the TMA producer (the stage's B tiles free), the A-operand warps (TMEM A stage free)
-// and the drain (accumulator ready) all wait on.  Stages are 128 points long so that the fixed
-// cost of a stage's barrier round trips is spread over 16 MMAs.  Every wait is bounded
+// and the drain (accumulator ready) all wait on.  Stages are 128 points long so that the
+// fixed cost of a stage's barrier round trips is spread over 16 MMAs.  Every wait is bounded
 // (globaltimer); on expiry the kernel records an error flag, stops issuing work, drains
 // its own MMAs and frees TMEM.
 #include <cuda.h>
@@ -56,7 +56,7 @@ constexpr int A_TILE = 4 * A_QUARTER;         // 32 KB: one source tile of a sta
 constexpr int NUM_WARPS = 18;                 // producer, MMA, 8 drain, 8 A-operand
 constexpr int THREADS = NUM_WARPS * 32;
 constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t ACC_COL = 0;               // accumulator b at 128 b: [0,64) hi*B+lo*Bhi, [64,128) hi*Blo
+constexpr uint32_t ACC_COL = 0;               // accumulator b at 128 b: [0,nc) hi*Bhi+lo*Bhi, [nc,2nc) hi*Blo
 constexpr uint32_t A_COL = 256;               // A stage a at 256 + 128 a: hi +0..63, lo +64..127
 // Points per work item: 32 768 when that still gives every SM at least kMinItemsPerSm
 // items (one CTA per SM walks them), else 16 384.  Longer slices spread the per-item
