@@ -15,7 +15,7 @@
 //     A stage's source tiles are refilled as soon as the A-operand warps have read
 //     them and its B tiles once the stage's MMAs completed, each part with its own
 //     "landed" barrier, so the sources get about one more stage of lead time;
-//   * warps 10..17 (2 per TMEM lane quadrant, one 64-point half each) read the
+//   * warps 10..25 (AGW = 4 per TMEM lane quadrant, one 32-point quarter each) read the
 //     row's F1_i, F2_j from SMEM (one 8-point group ahead of the math), form
 //     P = F1_i*F2_j with packed f32x2 arithmetic, split P = hi + lo (bf16
 //     round-to-nearest) and store them with tcgen05.st into the 2-stage TMEM
@@ -53,7 +53,11 @@ constexpr int B_TILE = kMaxCols * 128;        // 8 KB: 64 rows x 64 bf16 (one 64
 constexpr int B_BLOCK = 2 * B_TILE;           // 16 KB: hi then lo of one K block
 constexpr int A_QUARTER = kMaxSrcRows * 128;  // 8 KB: 64 rows x 32 fp32
 constexpr int A_TILE = 4 * A_QUARTER;         // 32 KB: one source tile of a stage
-constexpr int NUM_WARPS = 18;                 // producer, MMA, 8 drain, 8 A-operand
+// A-operand warps per TMEM lane quadrant, one 128 / AGW-point part of a stage each.  Their
+// shared-memory loads are latency-bound: 4 per quadrant ran 3.5% faster than 2, with 72
+// registers a thread instead of 96.
+constexpr int AGW = 4;
+constexpr int NUM_WARPS = 10 + 4 * AGW;       // producer, MMA, 8 drain, 4 AGW A-operand
 constexpr int THREADS = NUM_WARPS * 32;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_COL = 0;               // accumulator b at 128 b: [0,nc) hi*Bhi+lo*Bhi, [nc,2nc) hi*Blo
@@ -85,9 +89,9 @@ static_assert(ACC_CHUNKS == 1, "the drain waits on the per-stage completion");
 struct Bars {
   uint64_t full[MAX_SSTAGES];      // the stage's source tiles landed (TMA bytes)
   uint64_t full_b[MAX_SSTAGES];    // the stage's B tiles landed (TMA bytes)
-  uint64_t src_free[MAX_SSTAGES];  // the A-operand warps have read the stage's sources (8)
+  uint64_t src_free[MAX_SSTAGES];  // the A-operand warps have read the stage's sources (4 AGW)
   uint64_t done[DONE_RING];        // the MMAs of stage c completed (tcgen05.commit), c % 4
-  uint64_t afull[ASTAGES];         // A operand of the chunk is in TMEM (8 warp arrivals)
+  uint64_t afull[ASTAGES];         // A operand of the chunk is in TMEM (4 AGW warp arrivals)
   uint64_t accempty[NACC];
   uint64_t all_done;
   uint32_t tmem_base;
@@ -329,7 +333,7 @@ __device__ __forceinline__ void split2(unsigned long long p, uint32_t& hi, uint3
   lo = bf16x2_of(f2_sub(p, g));
 }
 
-// 18 warps: 5 share one SM sub-partition, whose 16K registers allow 102 per thread.
+// 26 warps: 7 share one SM sub-partition, whose 16K registers allow 73 per thread.
 template <bool kTwoSrc, bool kLongSlice>
 __global__ void __launch_bounds__(THREADS, 1)
     contract_tc_kernel(const __grid_constant__ Maps maps, const TileDesc* __restrict__ tiles,
@@ -354,11 +358,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int s = 0; s < SST; ++s) {
       mbar_init(&bars->full[s], 1);
       mbar_init(&bars->full_b[s], 1);
-      mbar_init(&bars->src_free[s], 8);
+      mbar_init(&bars->src_free[s], 4 * AGW);
 
     }
     for (int a = 0; a < ASTAGES; ++a) {
-      mbar_init(&bars->afull[a], 8);
+      mbar_init(&bars->afull[a], 4 * AGW);
 
     }
     for (int b = 0; b < NACC; ++b) {
@@ -554,7 +558,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   } else {
     // ------------------------------------------------------------ A-operand producers
     const int qd = warp & 3;
-    const int half = (warp - 10) >> 2;  // points [64 half, 64 half + 64) of a stage
+    constexpr int PPW = KCH / AGW, NG = PPW / 8;  // points per warp, 8-point groups
+    const int part = (warp - 10) >> 2;  // points [PPW part, PPW part + PPW) of a stage
     const int r = qd * 32 + lane;
     const uint32_t tlane = (uint32_t)(qd * 32) << 16;
     uint32_t chunk = 0;
@@ -588,20 +593,20 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         tc_fence_after();
         const uint8_t* st = smem + s * STAGE_BYTES;
-        const uint32_t a_hi = tmem + tlane + A_COL + a * 128 + half * 32;
-        // The warp's 64 points in 8 groups of 8; the shared-memory loads of group g + 1 are
-        // issued before the math of group g (software pipelining: the loads' latency, not
-        // the load pipe's bandwidth, bounds these warps).  Group g covers the 16-byte chunks
-        // c = 4 (sub & 1) + 2 (g & 1) + e (e < 2) of quarter 2 half + sub / 2 of the source
-        // tile, sub = g / 2; two groups fill one 16-point K step of the A operand.
+        const uint32_t a_hi = tmem + tlane + A_COL + a * 128 + part * (PPW / 2);
+        // The warp's PPW points in NG groups of 8; the shared-memory loads of group g + 1
+        // are issued before the math of group g (software pipelining: the loads' latency,
+        // not the load pipe's bandwidth, bounds these warps).  Group g (stage points p0 ..
+        // p0 + 7) covers the 16-byte chunks (p0 % 32) / 4 + e (e < 2) of 32-point quarter
+        // p0 / 32 of the source tile; two groups fill one 16-point K step of the A operand.
         auto load_group = [&](int g, ulonglong2 (&va)[2], ulonglong2 (&vb)[2]) {
-          const int sub = g >> 1;
-          const int qq = 2 * half + (sub >> 1);
+          const int p0 = part * PPW + 8 * g;
+          const int qq = p0 >> 5;
           const uint8_t* row1 = st + 2 * B_BLOCK + qq * qstride + pi * 128;
           const uint8_t* row2 = st + 2 * B_BLOCK + src2 + qq * qstride2 + pj * 128;
 #pragma unroll
           for (int e = 0; e < 2; ++e) {
-            const int c = (sub & 1) * 4 + (g & 1) * 2 + e;
+            const int c = ((p0 & 31) >> 2) + e;
             va[e] = *reinterpret_cast<const ulonglong2*>(row1 + ((c ^ (pi & 7)) << 4));
             vb[e] = *reinterpret_cast<const ulonglong2*>(row2 + ((c ^ (pj & 7)) << 4));
           }
@@ -610,8 +615,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         load_group(0, ca, cb);
         uint32_t hi[8], lo[8];
 #pragma unroll
-        for (int g = 0; g < 8; ++g) {
-          if (g + 1 < 8) load_group(g + 1, na, nb);
+        for (int g = 0; g < NG; ++g) {
+          if (g + 1 < NG) load_group(g + 1, na, nb);
 #pragma unroll
           for (int e = 0; e < 2; ++e) {
             const int c4 = (g & 1) * 2 + e;
