@@ -198,14 +198,6 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
       : "memory");
 }
-__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, uint64_t* bar,
-                                            int x, int y, int z, int w) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
-      : "memory");
-}
 __device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map, uint64_t* bar,
                                             int x, int y, int z, int w, int v) {
   asm volatile(
@@ -694,7 +686,7 @@ void make_map(CUtensorMap* m, CUtensorMapDataType dt, int esize, const void* bas
 
 // View of a [rows][K] array with K cut into blocks of `blk` points:
 // dims {blk, rows, K / blk}; box {blk, box_rows, nblk}.  Returns false (map unusable)
-// instead of failing when the driver rejects the layout.
+// instead of failing when the CUDA driver rejects the layout.
 bool make_block_map(CUtensorMap* m, CUtensorMapDataType dt, int esize, const void* base,
                     int64_t K, int rows, int blk, int box_rows, int nblk) {
   cuuint64_t dims[3] = {(cuuint64_t)blk, (cuuint64_t)rows, (cuuint64_t)(K / blk)};

@@ -1,6 +1,6 @@
 """FP64 CPU oracle for the FFT bispectrum path -- TEST INFRASTRUCTURE ONLY.
 
-This module is the checker for the GPU path.  Only ``tests/``,
+This module is the oracle for the GPU path.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may
 import it; the product (``bskit_gb300``) never does.
 
