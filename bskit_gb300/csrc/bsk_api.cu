@@ -460,15 +460,16 @@ void measure_b_stream(bsk_plan* p, const bsk_triset* set, int a, int b, int c, i
 
 void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int precision,
                int64_t k0, int64_t k1, double* out, cudaStream_t st) {
-  BSK_REQUIRE(p && set && out, BSK_ERR_ARG, "NULL argument");
+  BSK_REQUIRE(p && set, BSK_ERR_ARG, "NULL argument");
   BSK_REQUIRE(set->plan == p, BSK_ERR_ARG, "triangle set belongs to another plan");
   BSK_REQUIRE(a >= 0 && a < 3 && b >= 0 && b < 3 && c >= 0 && c < 3, BSK_ERR_ARG,
               "slot must be 0, 1 or 2");
   BSK_REQUIRE(0 <= k0 && k0 <= k1 && k1 <= p->K, BSK_ERR_ARG, "bad point range");
-  if (set->T == 0) return;
   const bool tc = precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16;
   BSK_REQUIRE(tc || precision == BSK_PREC_FP32 || precision == BSK_PREC_FP64, BSK_ERR_ARG,
               "unknown precision " + std::to_string(precision));
+  if (set->T == 0) return;  // nothing to write: out may be NULL
+  BSK_REQUIRE(out, BSK_ERR_ARG, "NULL argument");
   if (tc)
     BSK_REQUIRE(k0 % 128 == 0 && (k1 % 128 == 0 || k1 == p->K), BSK_ERR_ARG,
                 "tensor-core point ranges must start and end at multiples of 128 (or end at "
@@ -961,12 +962,16 @@ int bsk_measure_b_range(bsk_plan* p, const bsk_triset* set, int a, int b, int c,
 int bsk_contract(bsk_plan* p, const bsk_triset* set, const float* f1, const float* f2,
                  const float* f3, int64_t K, int precision, double* out, void* stream) {
   return guarded([&] {
-    BSK_REQUIRE(p && set && f1 && f2 && f3 && out, BSK_ERR_ARG, "NULL argument");
+    BSK_REQUIRE(p && set && f1 && f2 && f3, BSK_ERR_ARG, "NULL argument");
     BSK_REQUIRE(set->plan == p, BSK_ERR_ARG, "triangle set belongs to another plan");
     BSK_REQUIRE(K > 0 && K % 8 == 0, BSK_ERR_ARG, "k_points must be a positive multiple of 8");
+    BSK_REQUIRE(precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16 ||
+                    precision == BSK_PREC_FP32 || precision == BSK_PREC_FP64,
+                BSK_ERR_ARG, "unknown precision " + std::to_string(precision));
     DeviceGuard g(p->device);
     cudaStream_t st = (cudaStream_t)stream;
-    if (set->T == 0) return;
+    if (set->T == 0) return;  // nothing to write: out may be NULL
+    BSK_REQUIRE(out, BSK_ERR_ARG, "NULL argument");
     __nv_bfloat16* split = nullptr;
     if (precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16) {
       split = (__nv_bfloat16*)dmalloc_async(split_elems(p->n, K) * sizeof(__nv_bfloat16), st);
@@ -980,11 +985,12 @@ int bsk_contract(bsk_plan* p, const bsk_triset* set, const float* f1, const floa
 int bsk_gridinfo(bsk_plan* p, const bsk_triset* set, double* ntri, double* kmean,
                  void* stream) {
   return guarded([&] {
-    BSK_REQUIRE(p && set && ntri && kmean, BSK_ERR_ARG, "NULL argument");
+    BSK_REQUIRE(p && set, BSK_ERR_ARG, "NULL argument");
     BSK_REQUIRE(set->plan == p, BSK_ERR_ARG, "triangle set belongs to another plan");
     DeviceGuard g(p->device);
     cudaStream_t st = (cudaStream_t)stream;
-    if (set->T == 0) return;
+    if (set->T == 0) return;  // nothing to write: ntri and kmean may be NULL
+    BSK_REQUIRE(ntri && kmean, BSK_ERR_ARG, "NULL argument");
     make_z2d(p);
     bind_work(p, p->z2d, st);
     const size_t fbytes = (size_t)p->n_alloc() * p->K * sizeof(double);

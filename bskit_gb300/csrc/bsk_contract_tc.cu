@@ -39,6 +39,8 @@
 // its own MMAs and frees TMEM.
 #include <cuda.h>
 
+#include <atomic>
+
 #include "bsk_internal.cuh"
 
 namespace bsk {
@@ -656,16 +658,16 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
+  // resolved once (thread-safe static initialisation; a throw leaves it for the next call)
+  static const EncodeTiledFn fn = [] {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     BSK_CHECK_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
                                                     cudaEnableDefault, &q));
     BSK_REQUIRE(q == cudaDriverEntryPointSuccess && p, BSK_ERR_CUDA,
                 "cuTensorMapEncodeTiled entry point unavailable");
-    fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
   return fn;
 }
 
@@ -755,7 +757,7 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
   const int64_t n_slices = (k_end - k_begin + slice - 1) / slice;
   const int64_t n_items = n_slices * s.n_tiles;
   constexpr int kMaxDev = 64;
-  static bool attr_set[kMaxDev][4] = {};
+  static std::atomic<bool> attr_set[kMaxDev][4];  // zero-initialised: false
   int dev = 0;
   BSK_CHECK_CUDA(cudaGetDevice(&dev));
   BSK_REQUIRE(dev < kMaxDev, BSK_ERR_UNSUPPORTED, "device ordinal above 63");

@@ -24,6 +24,7 @@
 //  * requests that do not fit in the array are rejected with BSK_ERR_ARG.
 #include <algorithm>
 #include <map>
+#include <mutex>
 
 #include "bsk_internal.cuh"
 
@@ -35,9 +36,11 @@ static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBy
 
 constexpr int kMaxDevices = 64;
 void* g_scratch_ptr[kMaxDevices] = {nullptr};
+std::mutex g_scratch_mutex;  // first calls from several host threads resolve the address once
 
 void* scratch_address(int dev) {
   BSK_REQUIRE(dev >= 0 && dev < kMaxDevices, BSK_ERR_UNSUPPORTED, "device ordinal above 63");
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
   if (!g_scratch_ptr[dev]) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);

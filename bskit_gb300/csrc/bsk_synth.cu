@@ -14,6 +14,7 @@
 // runs of it.
 // The FFTs are radix-8/4/2/3/5 Stockham passes in shared memory (twiddles from a table
 // computed in double precision on the host); unnormalised, sign +1, as cuFFT's C2R.
+#include <atomic>
 #include <cmath>
 
 #include "bsk_internal.cuh"
@@ -583,7 +584,7 @@ __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPl
 template <int NC>
 void run_synth(const SynthArgs& A, const FftPlan& pl, int nk, int Cp, int ns, size_t fft_smem,
                size_t x_smem, cudaStream_t st) {
-  static bool attr_done[64] = {};
+  static std::atomic<bool> attr_done[64];  // zero-initialised: false
   int dev = 0;
   BSK_CHECK_CUDA(cudaGetDevice(&dev));
   if (dev < 64 && !attr_done[dev]) {

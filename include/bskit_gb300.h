@@ -111,7 +111,10 @@ int bsk_shell_mode_counts(const bsk_plan* plan, int64_t* counts);
 
 /*
  * Register a list of T triangle bins (host int32 [T][3] shell indices) and
- * build its contraction schedule on the plan's device.
+ * build its contraction schedule on the plan's device.  T may be 0 (tri may
+ * then be NULL): bsk_measure_b(_range), bsk_gridinfo and bsk_contract check
+ * their other arguments, launch nothing and accept NULL output pointers for an
+ * empty set, as bskit's measurement loops run zero times for imin == imax.
  * Replaces: FFTBispectrum.k_indices set-up, bskit/main.py:1553-1584.
  */
 int bsk_triset_create(bsk_plan* plan, int64_t n_tri, const int32_t* tri, bsk_triset** out);

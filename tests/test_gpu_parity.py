@@ -201,6 +201,43 @@ def test_contract_ragged_grid_matches_fp64(cuda):
     plan.sync_check()
 
 
+def test_empty_set_and_single_shell(cuda):
+    # an empty triangle list through every measuring entry point (torch hands out NULL
+    # data pointers for empty tensors), then one shell and its one bin (0, 0, 0)
+    n, box = 32, 100.0
+    kf = TWO_PI / box
+    edges = np.array([[2 * kf, 4 * kf]])
+    delta = synthetic.lognormal_mesh(n, box, seed=14)
+    plan = Plan(n, box, edges)
+    plan.paint(0, torch.from_numpy(delta))
+    empty = plan.triangles(np.zeros((0, 3), np.int32))
+    assert empty.T == 0
+    for prec in ("fp64", "fp32", "bf16x3", "bf16"):
+        assert plan.measure_b(empty, precision=prec).numel() == 0
+    nt, km = plan.gridinfo(empty)
+    assert nt.numel() == 0 and tuple(km.shape) == (0, 3)
+    f = torch.ones((1, 1024), device="cuda")
+    assert plan.contract(empty, f, f, f).numel() == 0
+    assert Plan.normalize(nt, nt).numel() == 0
+    plan.sync_check()
+
+    tri = np.array([[0, 0, 0]], np.int32)
+    ts = plan.triangles(tri)
+    of = O.shell_fields(O.spectrum(delta), n, box, edges)
+    bo = O.triple_sums(of, of, of, tri) * box ** 6 / n ** 3
+    babs = _abs_sums(of, of, of, tri, box, n)
+    # one bin: the normalised bounds alone (a median over one bin is that bin's relative error)
+    for prec, bound in (("fp64", 2e-6), ("fp32", 2e-6), ("bf16x3", 4e-6), ("bf16", 1e-3)):
+        b = plan.measure_b(ts, precision=prec)
+        plan.sync_check()
+        assert (np.abs(b.cpu().numpy() - bo) / babs).max() <= bound, prec
+    nt, km = plan.gridinfo(ts)
+    plan.sync_check()
+    _, nto, kmo = O.grid_info(n, box, edges, tri)
+    assert np.array_equal(nt.cpu().numpy(), nto) and nto[0] > 0
+    assert np.allclose(km.cpu().numpy(), kmo, rtol=1e-12, atol=0)
+
+
 @pytest.mark.parametrize("prec", ["fp64", "bf16x3"])
 def test_cross_bispectra(cuda, prec):
     n, box = 48, 100.0
