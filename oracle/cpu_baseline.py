@@ -1,7 +1,7 @@
 """Timed CPU restatement of bskit's fast path -- TEST/BENCH INFRASTRUCTURE ONLY.
 
-Only bench.py's ``cpu_baseline`` leg and its ``--impl reference`` arm use this
-module.  It times, on the host cores, the reference algorithm of
+Only bench.py's ``cpu_baseline`` leg, its ``--impl reference`` arm and ``tests/``
+(which check that the sampled work is the reference's work) use this module.  It times, on the host cores, the reference algorithm of
 ``FFTBispectrum.measure_bispectrum_faster`` (bskit/main.py:1846-1879) the way
 bskit runs it under MPI:
 
@@ -99,9 +99,10 @@ class ReferenceCPU(object):
         parts = self.pool.map(_slab_sums, [(self.bounds[i], self.bounds[i + 1], self.loc)
                                            for i in range(self.P)])
         t_tri = time.perf_counter() - t0
-        np.sum(parts, axis=0)
+        sums = np.sum(parts, axis=0)  # the host-side sum over slabs (main.py:1878-1879)
         est = len(self.edges) * t_fft / self.P + self.t_r2c / self.P + self.T * t_tri / len(self.loc)
-        self.last = {"t_c2r_s": t_fft, "t_triangle_sample_s": t_tri, "sample_seconds": t_fft + t_tri}
+        self.last = {"t_c2r_s": t_fft, "t_triangle_sample_s": t_tri, "sample_seconds": t_fft + t_tri,
+                     "sums": sums}
         return est
 
     def describe(self):
