@@ -1,7 +1,8 @@
 """Timed CPU restatement of bskit's fast path -- TEST/BENCH INFRASTRUCTURE ONLY.
 
 Only bench.py's ``cpu_baseline`` leg, its ``--impl reference`` arm and ``tests/``
-(which check that the sampled work is the reference's work) use this module.  It times, on the host cores, the reference algorithm of
+(which check that the sampled work is the reference's work) use this module.
+It times, on the host cores, the reference algorithm of
 ``FFTBispectrum.measure_bispectrum_faster`` (bskit/main.py:1846-1879) the way
 bskit runs it under MPI:
 
