@@ -24,6 +24,15 @@ def _require_cuda():
         raise RuntimeError("bskit_gb300 computes on a CUDA device only (none is available)")
 
 
+def _check_tensor(t, what, shape, dtype, device):
+    """A device buffer handed to the C ABI as a raw pointer: the kernels trust its size, so
+    the shape, dtype, device and layout are checked here."""
+    if (not isinstance(t, torch.Tensor) or tuple(t.shape) != tuple(shape) or t.dtype != dtype
+            or t.device != device or not t.is_contiguous()):
+        raise ValueError("%s must be a contiguous %s tensor of shape %s on %s" %
+                         (what, dtype, tuple(shape), device))
+
+
 class TriangleSet:
     """A registered list of (i, j, l) shell-index triples (``k_indices`` rows)."""
 
@@ -135,6 +144,7 @@ class Plan:
         prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         if out is None:
             out = torch.empty(tset.T, dtype=torch.float64, device=self.device)
+        _check_tensor(out, "out", (tset.T,), torch.float64, self.device)
         with torch.cuda.device(self.device):
             _lib.call("bsk_measure_b", self.handle, tset.handle, int(slots[0]), int(slots[1]),
                       int(slots[2]), prec, ctypes.c_void_p(out.data_ptr()), _stream_ptr(stream))
@@ -146,6 +156,7 @@ class Plan:
         prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         if out is None:
             out = torch.empty(tset.T, dtype=torch.float64, device=self.device)
+        _check_tensor(out, "out", (tset.T,), torch.float64, self.device)
         with torch.cuda.device(self.device):
             _lib.call("bsk_measure_b_range", self.handle, tset.handle, int(slots[0]),
                       int(slots[1]), int(slots[2]), prec, int(k_begin), int(k_end),
@@ -165,10 +176,11 @@ class Plan:
         """Raw contraction of caller fields ([n][K] float32 CUDA): sum_k f1 f2 f3."""
         prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         fs = [f.contiguous() for f in (f1, f2, f3)]
-        for f in fs:
-            if f.dtype != torch.float32 or not f.is_cuda or f.shape[0] != self.n_shells:
-                raise ValueError("fields must be float32 CUDA tensors of shape (n_shells, K)")
-        K = fs[0][0].numel()
+        if fs[0].dim() != 2:
+            raise ValueError("fields must be float32 CUDA tensors of shape (n_shells, K)")
+        K = fs[0].shape[1]
+        for i, f in enumerate(fs):
+            _check_tensor(f, "f%d" % (i + 1), (self.n_shells, K), torch.float32, self.device)
         out = torch.empty(tset.T, dtype=torch.float64, device=self.device)
         with torch.cuda.device(self.device):
             _lib.call("bsk_contract", self.handle, tset.handle, *[ctypes.c_void_p(f.data_ptr())
@@ -190,10 +202,17 @@ class Plan:
 
     @staticmethod
     def normalize(b_unnorm, ntri, stream=None):
+        """b_unnorm / ntri (float64 CUDA tensors of one length T)."""
+        if not isinstance(b_unnorm, torch.Tensor) or not b_unnorm.is_cuda:
+            raise ValueError("b_unnorm must be a float64 CUDA tensor")
+        dev, T = b_unnorm.device, b_unnorm.numel()
+        _check_tensor(b_unnorm, "b_unnorm", (T,), torch.float64, dev)
+        _check_tensor(ntri, "ntri", (T,), torch.float64, dev)
         out = torch.empty_like(b_unnorm)
-        _lib.call("bsk_normalize", int(b_unnorm.numel()), ctypes.c_void_p(b_unnorm.data_ptr()),
-                  ctypes.c_void_p(ntri.data_ptr()), ctypes.c_void_p(out.data_ptr()),
-                  _stream_ptr(stream))
+        with torch.cuda.device(dev):
+            _lib.call("bsk_normalize", int(b_unnorm.numel()), ctypes.c_void_p(b_unnorm.data_ptr()),
+                      ctypes.c_void_p(ntri.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                      _stream_ptr(stream))
         return out
 
     # ------------------------------------------------------------------ helpers
@@ -238,6 +257,7 @@ def compensate_cic(mesh, nmesh_cic, out=None, stream=None):
         m = m.cuda()
     if out is None:
         out = torch.empty_like(m)
+    _check_tensor(out, "out", tuple(m.shape), torch.float32, m.device)
     with torch.cuda.device(m.device):
         _lib.call("bsk_compensate_cic", int(m.shape[0]), int(nmesh_cic),
                   ctypes.c_void_p(m.data_ptr()), ctypes.c_void_p(out.data_ptr()),

@@ -62,3 +62,23 @@ def test_bad_arguments_rejected_without_gpu(lib):
     assert lib.bsk_plan_create(64, 100.0, 0, edges, 0, 0, ctypes.byref(out)) == _lib.BSK_ERR_ARG
     assert lib.bsk_plan_create(64, 100.0, 1, edges, 7, 0, ctypes.byref(out)) == _lib.BSK_ERR_ARG
     assert lib.bsk_normalize(-1, None, None, None, None) == _lib.BSK_ERR_ARG
+
+
+def test_host_checks_reject_bad_buffers():
+    # buffers go to the kernels as raw pointers, so the object layer checks their size,
+    # type, device and layout first (no GPU needed: these fail before any library call)
+    import torch
+
+    from bskit_gb300 import engine
+
+    cpu = torch.device("cpu")
+    good = torch.zeros(5, dtype=torch.float64)
+    engine._check_tensor(good, "out", (5,), torch.float64, cpu)
+    for bad in (torch.zeros(4, dtype=torch.float64), torch.zeros(5, dtype=torch.float32),
+                torch.zeros(10, dtype=torch.float64)[::2], [0.0] * 5):
+        with pytest.raises(ValueError):
+            engine._check_tensor(bad, "out", (5,), torch.float64, cpu)
+    with pytest.raises(ValueError):
+        engine._check_tensor(good, "out", (5,), torch.float64, torch.device("cuda", 0))
+    with pytest.raises(ValueError):
+        engine.Plan.normalize(good, good)  # host tensors
