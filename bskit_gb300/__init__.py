@@ -7,12 +7,13 @@ sm_103a CUDA library ``libbskit_gb300.so`` through its C ABI.
 from .bins import (generate_bin_edge_list, generate_equilateral_triangle_bin_list,
                    generate_isosceles_triangle_bin_list, generate_squeezed_triangle_bin_list,
                    generate_triangle_bin_list, geometric_k_mean, triangle_indices_to_edges)
+from .bigfile import BigFileMesh
 from .mesh import ArrayMesh, as_mesh
 
 __version__ = "0.1.0"
 
 __all__ = [
-    "FFTBispectrum", "ArrayMesh", "as_mesh", "Plan", "TriangleSet",
+    "FFTBispectrum", "ArrayMesh", "BigFileMesh", "as_mesh", "Plan", "TriangleSet",
     "generate_bin_edge_list", "generate_equilateral_triangle_bin_list",
     "generate_isosceles_triangle_bin_list", "generate_squeezed_triangle_bin_list",
     "generate_triangle_bin_list", "geometric_k_mean", "triangle_indices_to_edges",
