@@ -42,6 +42,9 @@ int guarded(F&& f) {
   } catch (const std::exception& e) {
     g_err = e.what();
     return BSK_ERR_ARG;
+  } catch (...) {  // nothing may unwind through the C ABI
+    g_err = "unexpected exception";
+    return BSK_ERR_STATE;
   }
 }
 

@@ -197,8 +197,14 @@ extern "C" int bsk_contract_noalloc(int n_shells, int64_t n_tri, const int32_t* 
   } catch (const Error& e) {
     set_error(e.msg);
     return e.code;
+  } catch (const std::bad_alloc&) {  // the host-side tiling tables
+    set_error("host allocation failed");
+    return BSK_ERR_OOM;
   } catch (const std::exception& e) {
     set_error(e.what());
     return BSK_ERR_ARG;
+  } catch (...) {  // nothing may unwind through the C ABI
+    set_error("unexpected exception");
+    return BSK_ERR_STATE;
   }
 }
