@@ -31,6 +31,7 @@ import numpy as np
 from . import bins as _bins
 
 TRIANGLE_TYPES = ("all", "equilateral", "squeezed", "isosceles")
+PRECISIONS = ("bf16x3", "fp32", "bf16", "fp64")
 
 
 class Request(object):
@@ -42,6 +43,14 @@ class Request(object):
     """
 
     def __init__(self, rid, mesh, box, spec, second=None, precision="bf16x3", arrival=0.0):
+        # checked here, at submission: a bad request must not fail later inside a batch
+        for m in (mesh, second):
+            if m is not None and (len(m.shape) != 3 or len(set(m.shape)) != 1):
+                raise ValueError("meshes must be cubic N^3 arrays")
+        if second is not None and tuple(second.shape) != tuple(mesh.shape):
+            raise ValueError("the second mesh must have the first mesh's shape")
+        if precision not in PRECISIONS:
+            raise ValueError("precision must be one of %s" % (PRECISIONS,))
         self.rid = rid
         self.mesh = mesh
         self.second = second

@@ -105,6 +105,21 @@ def test_requests_never_exceed_budget_wait_instead():
     assert all(k == 1 for _, k in be.launched)
 
 
+def test_bad_requests_rejected_at_submission():
+    kf = 2 * np.pi / 100.0
+    spec = dict(kmin=kf, kmax=4 * kf, dk=2 * kf)
+    cube = np.zeros((16,) * 3, np.float32)
+    for kw in (dict(mesh=np.zeros((16, 16, 8), np.float32)),
+               dict(mesh=np.zeros((16, 16), np.float32)),
+               dict(mesh=cube, second=np.zeros((8,) * 3, np.float32)),
+               dict(mesh=cube, precision="fp16")):
+        with pytest.raises(ValueError):
+            serving.Request(0, box=100.0, spec=spec, **kw)
+    with pytest.raises(ValueError):  # an unknown triangle type fails when submitted
+        serving.Scheduler(FakeBackend(), 1 << 30).submit(
+            serving.Request(0, cube, 100.0, dict(spec, triangle_type="obtuse")))
+
+
 def test_cross_requests_have_their_own_bin_set():
     be = FakeBackend()
     sch = serving.Scheduler(be, mem_budget=10 ** 6, max_batch=4, clock=FakeClock())
