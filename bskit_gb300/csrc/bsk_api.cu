@@ -477,6 +477,10 @@ void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int prec
     BSK_REQUIRE(k0 % 128 == 0 && (k1 % 128 == 0 || k1 == p->K), BSK_ERR_ARG,
                 "tensor-core point ranges must start and end at multiples of 128 (or end at "
                 "the whole grid)");
+  if (k0 == k1) {  // an empty share of the grid (more ranks than 128-point stages): zeros
+    BSK_CHECK_CUDA(cudaMemsetAsync(out, 0, (size_t)set->T * sizeof(double), st));
+    return;
+  }
   if (p->mem_budget) {
     // resident path: all shells of each slot (and the split of the third) stay on the device
     const size_t field_bytes = (size_t)p->n_alloc() * p->K * sizeof(float);

@@ -345,6 +345,19 @@ def test_slab_ranges_sum_to_whole(cuda):
         assert np.abs(tot - whole).max() <= tol * np.abs(whole).max(), prec
 
 
+def test_empty_point_range_is_zero(cuda):
+    # a rank whose share of the grid is empty (more ranks than 128-point stages) adds zeros
+    n, box, edges, tri = _small(32, 100.0, 2)
+    plan = Plan(n, box, edges)
+    plan.paint(0, torch.from_numpy(synthetic.lognormal_mesh(n, box, seed=15)))
+    ts = plan.triangles(tri)
+    for prec in ("fp64", "fp32", "bf16x3"):
+        out = torch.full((len(tri),), 7.0, dtype=torch.float64, device="cuda")
+        plan.measure_b_range(ts, 256, 256, precision=prec, out=out)
+        plan.sync_check()
+        assert torch.count_nonzero(out).item() == 0, prec
+
+
 def test_schedule_covers_every_pair(cuda):
     n, box, edges, tri = _small(64, 100.0, 2, 0.25)
     plan = Plan(n, box, edges)
