@@ -76,9 +76,23 @@ struct HostTriangle {
   int i, j, l;
 };
 
-// Build the tile schedule for a triangle list (host).  `n_shells` bounds the
-// indices.  Rows with identical (i, j) share one pair product.  Map entries are
+// The tile schedule of a triangle list in host memory: per tile a TileDesc, kTileRows
+// pair-row shells (-1 = padding) and an nc x kTileRows map of triangle indices (-1 = not
+// a bin).
+struct HostSchedule {
+  std::vector<TileDesc> tiles;
+  std::vector<int16_t> ri, rj;
+  std::vector<int32_t> map;
+  int sum_nc = 0;
+};
+
+// Tile a triangle list (host only).  `n_shells` bounds the indices.  Rows with identical
+// (i, j) share one pair product; the list must not repeat an (i, j, l).  Map entries are
 // positions in `tri`, or map_index[position] when map_index is given.
+void tile_schedule(const std::vector<HostTriangle>& tri, int n_shells,
+                   const std::vector<int>* map_index, HostSchedule& out);
+
+// tile_schedule, uploaded to the device (with the SIMT kernels' sub-tile list).
 void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSchedule& out,
                     const std::vector<int>* map_index = nullptr);
 

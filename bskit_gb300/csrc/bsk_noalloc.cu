@@ -23,8 +23,9 @@
 //    the GPU (different streams, no ordering) race on the array;
 //  * requests that do not fit in the array are rejected with BSK_ERR_ARG.
 #include <algorithm>
-#include <map>
 #include <mutex>
+#include <set>
+#include <tuple>
 
 #include "bsk_internal.cuh"
 
@@ -56,78 +57,21 @@ void* scratch_address(int dev) {
 
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
-// Host-side tiling of the triangle list (rows = (i, j) pairs in order of first
-// appearance, 128 per tile, column span and pair-factor spans of at most 64
-// shells) into the layouts contract_tc_kernel reads.
-struct Tables {
-  std::vector<TileDesc> tiles;
-  std::vector<int16_t> ri, rj;
-  std::vector<int32_t> map;
-};
-
-void tile_triangles(int64_t T, const int32_t* tri, int n, Tables& out) {
-  std::map<std::pair<int, int>, int> row_of;
-  std::vector<std::pair<int, int>> rows;
-  std::vector<std::vector<std::pair<int, int>>> cols;  // per row: (l, t)
+// The triangle list as the shared tiler takes it.  A repeated (i, j, l) would put two
+// triangles in one schedule entry, so it is rejected (the plan path maps repeats onto
+// their first occurrence instead).
+std::vector<HostTriangle> checked_triangles(int64_t T, const int32_t* tri, int n) {
+  std::vector<HostTriangle> out;
+  out.reserve((size_t)T);
+  std::set<std::tuple<int, int, int>> seen;
   for (int64_t t = 0; t < T; ++t) {
     const int i = tri[3 * t], j = tri[3 * t + 1], l = tri[3 * t + 2];
     BSK_REQUIRE(i >= 0 && j >= 0 && l >= 0 && i < n && j < n && l < n, BSK_ERR_ARG,
                 "triangle " + std::to_string(t) + " has a shell index outside [0, n_shells)");
-    auto key = std::make_pair(i, j);
-    auto it = row_of.find(key);
-    int r;
-    if (it == row_of.end()) {
-      r = (int)rows.size();
-      row_of.emplace(key, r);
-      rows.push_back(key);
-      cols.emplace_back();
-    } else {
-      r = it->second;
-    }
-    for (const auto& c : cols[r])
-      BSK_REQUIRE(c.first != l, BSK_ERR_ARG, "repeated triangle in the list");
-    cols[r].emplace_back(l, (int)t);
+    BSK_REQUIRE(seen.emplace(i, j, l).second, BSK_ERR_ARG, "repeated triangle in the list");
+    out.push_back(HostTriangle{i, j, l});
   }
-  auto round16 = [](int v) { return std::max(16, (v + 15) / 16 * 16); };
-  auto round8 = [](int v) { return (v + 7) / 8 * 8; };
-  size_t r = 0;
-  while (r < rows.size()) {
-    int lmin = 1 << 30, lmax = -1, lo = 1 << 30, hi = -1;
-    size_t e = r;
-    while (e < rows.size() && e - r < (size_t)kTileRows) {
-      int nlmin = lmin, nlmax = lmax;
-      for (const auto& c : cols[e]) {
-        nlmin = std::min(nlmin, c.first);
-        nlmax = std::max(nlmax, c.first);
-      }
-      const int nlo = std::min(lo, std::min(rows[e].first, rows[e].second));
-      const int nhi = std::max(hi, std::max(rows[e].first, rows[e].second));
-      if (e > r && (round16(nlmax - nlmin + 1) > kMaxCols || nhi - nlo >= kMaxSrcRows)) break;
-      lmin = nlmin; lmax = nlmax; lo = nlo; hi = nhi;
-      ++e;
-    }
-    BSK_REQUIRE(round16(lmax - lmin + 1) <= kMaxCols && hi - lo < kMaxSrcRows,
-                BSK_ERR_UNSUPPORTED, "a pair row needs more than 64 column shells");
-    TileDesc d{};
-    d.i0 = d.j0 = lo;
-    d.ni = d.nj = round8(hi - lo + 1);
-    d.l0 = lmin;
-    d.nc = round16(lmax - lmin + 1);
-    d.nrows = (int)(e - r);
-    d.row_off = (int)out.ri.size();
-    d.map_off = (int)out.map.size();
-    out.ri.resize(out.ri.size() + kTileRows, (int16_t)-1);
-    out.rj.resize(out.rj.size() + kTileRows, (int16_t)-1);
-    out.map.resize(out.map.size() + (size_t)d.nc * kTileRows, -1);
-    for (size_t k = r; k < e; ++k) {
-      out.ri[d.row_off + (k - r)] = (int16_t)rows[k].first;
-      out.rj[d.row_off + (k - r)] = (int16_t)rows[k].second;
-      for (const auto& c : cols[k])
-        out.map[d.map_off + (size_t)(c.first - lmin) * kTileRows + (k - r)] = c.second;
-    }
-    out.tiles.push_back(d);
-    r = e;
-  }
+  return out;
 }
 
 }  // namespace
@@ -154,8 +98,8 @@ extern "C" int bsk_contract_noalloc(int n_shells, int64_t n_tri, const int32_t* 
     int num_sms = 0;
     BSK_CHECK_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
 
-    Tables tb;
-    tile_triangles(n_tri, tri, n_shells, tb);
+    HostSchedule tb;
+    tile_schedule(checked_triangles(n_tri, tri, n_shells), n_shells, nullptr, tb);
     const size_t b_tiles = align256(tb.tiles.size() * sizeof(TileDesc));
     const size_t b_rows = align256(tb.ri.size() * sizeof(int16_t));
     const size_t b_map = align256(tb.map.size() * sizeof(int32_t));

@@ -40,9 +40,8 @@ struct Row {
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 }  // namespace
 
-void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSchedule& out,
-                    const std::vector<int>* map_index) {
-  out.release();
+void tile_schedule(const std::vector<HostTriangle>& tri, int n_shells,
+                   const std::vector<int>* map_index, HostSchedule& out) {
   std::map<std::pair<int, int>, int> index;
   std::vector<Row> rows;
   for (size_t t = 0; t < tri.size(); ++t) {
@@ -64,6 +63,31 @@ void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSc
     R.lmin = std::min(R.lmin, h.l);
     R.lmax = std::max(R.lmax, h.l);
     R.cols.emplace_back(h.l, map_index ? (*map_index)[t] : (int)t);
+  }
+  // A tile holds at most kMaxCols column shells, so a pair whose third shells span more
+  // (possible with more than kMaxCols shells) becomes several rows, each over a run of at
+  // most kMaxCols consecutive shells.  With kMaxCols shells or fewer nothing is cut.
+  {
+    std::vector<Row> cut;
+    cut.reserve(rows.size());
+    for (Row& R : rows) {
+      if (R.lmax - R.lmin + 1 <= kMaxCols) {
+        cut.push_back(std::move(R));
+        continue;
+      }
+      std::sort(R.cols.begin(), R.cols.end());
+      Row seg{R.i, R.j, R.cols[0].first, R.cols[0].first, {}};
+      for (const auto& c : R.cols) {
+        if (c.first - seg.lmin + 1 > kMaxCols) {
+          cut.push_back(std::move(seg));
+          seg = Row{R.i, R.j, c.first, c.first, {}};
+        }
+        seg.lmax = c.first;
+        seg.cols.push_back(c);
+      }
+      cut.push_back(std::move(seg));
+    }
+    rows.swap(cut);
   }
   std::sort(rows.begin(), rows.end(), [](const Row& a, const Row& b) {
     if (a.lmax != b.lmax) return a.lmax < b.lmax;
@@ -100,9 +124,14 @@ void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSc
     if (!cur.empty()) groups.push_back(cur);
   }
 
-  std::vector<TileDesc> tiles;
-  std::vector<int16_t> ri, rj;
-  std::vector<int32_t> map;
+  std::vector<TileDesc>& tiles = out.tiles;
+  std::vector<int16_t>& ri = out.ri;
+  std::vector<int16_t>& rj = out.rj;
+  std::vector<int32_t>& map = out.map;
+  tiles.clear();
+  ri.clear();
+  rj.clear();
+  map.clear();
   int sum_nc = 0;
   for (auto& g : groups) {
     TileDesc d{};
@@ -123,6 +152,8 @@ void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSc
       d.nj = round_up(jmax - jmin + 1, 8);
     }
     d.nc = std::max(16, round_up(lmax - lmin + 1, 16));
+    BSK_REQUIRE(d.nc <= kMaxCols && d.ni <= kMaxSrcRows && d.nj <= kMaxSrcRows, BSK_ERR_STATE,
+                "internal: a tile exceeds its column or source span");
     d.nrows = (int)g.size();
     d.row_off = (int)ri.size();
     d.map_off = (int)map.size();
@@ -138,8 +169,20 @@ void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSc
     }
     tiles.push_back(d);
   }
-  out.n_tiles = (int)tiles.size();
   out.sum_nc = sum_nc;
+}
+
+void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSchedule& out,
+                    const std::vector<int>* map_index) {
+  out.release();
+  HostSchedule hs;
+  tile_schedule(tri, n_shells, map_index, hs);
+  const std::vector<TileDesc>& tiles = hs.tiles;
+  const std::vector<int16_t>& ri = hs.ri;
+  const std::vector<int16_t>& rj = hs.rj;
+  const std::vector<int32_t>& map = hs.map;
+  out.n_tiles = (int)tiles.size();
+  out.sum_nc = hs.sum_nc;
   out.h_tiles = tiles;
   if (tiles.empty()) return;
   BSK_CHECK_CUDA(cudaMalloc(&out.tiles, tiles.size() * sizeof(TileDesc)));

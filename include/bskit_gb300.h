@@ -123,9 +123,10 @@ int bsk_triset_destroy(bsk_triset* set);
 int64_t bsk_triset_size(const bsk_triset* set);
 /*
  * Contraction schedule of a set: out[0] = tiles (128 pair rows each), out[1] = sum of
- * the tiles' column counts, out[2] = distinct (i, j) pair rows.  The tensor-core
- * contraction issues 2 x 128 x 3 x out[1] flops per grid point for bf16x3 (useful:
- * 2 x T).  Diagnostics; no counterpart in the reference.
+ * the tiles' column counts, out[2] = pair rows: the distinct (i, j), a pair whose
+ * third shells span more than a tile's 64 columns counting once per run of at most 64.
+ * The tensor-core contraction issues 2 x 128 x 3 x out[1] flops per grid point for
+ * bf16x3 (useful: 2 x T).  Diagnostics; no counterpart in the reference.
  */
 int bsk_triset_schedule(const bsk_triset* set, int64_t* out);
 

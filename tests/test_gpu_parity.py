@@ -358,6 +358,35 @@ def test_empty_point_range_is_zero(cuda):
         assert torch.count_nonzero(out).item() == 0, prec
 
 
+def test_more_than_64_shells(cuda):
+    # 80 shells: a pair whose third shells span more than a tile's 64 columns becomes several
+    # GEMM rows, and a pair 65 shells apart takes two source ranges; the tensor-core
+    # contraction of random fields against the FP64 one of the same fields
+    n_sh, K = 80, 24 ** 3
+    kf = TWO_PI / 100.0
+    edges = np.array([[0.3 * s, 0.3 * s + 0.3] for s in range(n_sh)]) * kf
+    tri = ([(79, 79, l) for l in range(n_sh)] + [(70, 5, l) for l in range(0, n_sh, 2)] +
+           [(10, 12, l) for l in range(0, n_sh, 7)] + [(0, 0, 0)])
+    tri = np.array(tri, dtype=np.int32)
+    plan = Plan(64, 100.0, edges)
+    ts = plan.triangles(tri)
+    tiles, sum_nc, rows = ts.schedule()
+    assert rows == 7 and sum_nc <= 64 * tiles  # (79,79), (70,5), (10,12): two runs each
+    g = torch.Generator(device="cuda")
+    g.manual_seed(16)
+    fs = [torch.randn((n_sh, K), generator=g, device="cuda") for _ in range(3)]
+    b64 = plan.contract(ts, *fs, precision="fp64").cpu().numpy()
+    babs = plan.contract(ts, *[f.abs() for f in fs], precision="fp64").cpu().numpy()
+    want = np.array([np.dot(fs[0][i].double().cpu().numpy() * fs[1][j].double().cpu().numpy(),
+                            fs[2][l].double().cpu().numpy()) for i, j, l in tri])
+    assert np.abs(b64 - want).max() <= 1e-12 * babs.max()
+    for prec, bound in (("bf16x3", 4e-6), ("bf16", 1e-3)):
+        b = plan.contract(ts, *fs, precision=prec).cpu().numpy()
+        assert np.all(np.isfinite(b))
+        assert (np.abs(b - b64) / babs).max() <= bound, prec
+    plan.sync_check()
+
+
 def test_schedule_covers_every_pair(cuda):
     n, box, edges, tri = _small(64, 100.0, 2, 0.25)
     plan = Plan(n, box, edges)
