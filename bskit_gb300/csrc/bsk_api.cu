@@ -85,6 +85,35 @@ void* dmalloc_async(size_t bytes, cudaStream_t st) {
   return p;
 }
 
+// A stream-ordered device temporary that an error unwinding the call also releases.
+// release() is the success path: it frees at that point and reports a failure.
+struct AsyncTemp {
+  void* ptr = nullptr;
+  cudaStream_t st = nullptr;
+  AsyncTemp(size_t bytes, cudaStream_t s) : ptr(dmalloc_async(bytes, s)), st(s) {}
+  ~AsyncTemp() {
+    if (ptr) cudaFreeAsync(ptr, st);
+  }
+  void release() {
+    void* q = ptr;
+    ptr = nullptr;
+    BSK_CHECK_CUDA(cudaFreeAsync(q, st));
+  }
+  AsyncTemp(const AsyncTemp&) = delete;
+  AsyncTemp& operator=(const AsyncTemp&) = delete;
+};
+
+// The same for a synchronous allocation, freed when the scope ends.
+struct SyncTemp {
+  void* ptr = nullptr;
+  explicit SyncTemp(size_t bytes) : ptr(dmalloc(bytes)) {}
+  ~SyncTemp() {
+    if (ptr) cudaFree(ptr);
+  }
+  SyncTemp(const SyncTemp&) = delete;
+  SyncTemp& operator=(const SyncTemp&) = delete;
+};
+
 void grow_work(bsk_plan* p, size_t ws) {
   if (ws <= p->work_bytes) return;
   if (p->work) cudaFree(p->work);
@@ -236,6 +265,16 @@ void free_slot(FieldSlot& f) {
   if (f.fields) cudaFree(f.fields);
   if (f.split) cudaFree(f.split);
   f = FieldSlot{};
+}
+
+void destroy_triset(bsk_triset* set) {
+  if (!set) return;
+  DeviceGuard g(set->plan->device);
+  set->sched.release();
+  for (auto& kv : set->groups)
+    for (auto& g : kv.second) g.sched.release();
+  if (set->dups) cudaFree(set->dups);
+  delete set;
 }
 
 void destroy_plan(bsk_plan* p) {
@@ -554,9 +593,12 @@ void gridinfo_stream(bsk_plan* p, const bsk_triset* set, double* ntri, double* k
               "grid information: the budget of " + std::to_string(p->mem_budget) +
                   " bytes leaves room for no chunk of " + std::to_string(p->chunk) + " shells");
   const size_t buf_elems = (size_t)C * p->K;
-  double* pool = (double*)dmalloc_async(6 * buf_elems * sizeof(double), st);
-  cufftDoubleComplex* spec = (cufftDoubleComplex*)dmalloc_async(spec_bytes, st);
-  double* s1 = (double*)dmalloc_async(3 * (size_t)set->T * sizeof(double), st);
+  AsyncTemp pool_t(6 * buf_elems * sizeof(double), st);
+  AsyncTemp spec_t(spec_bytes, st);
+  AsyncTemp s1_t(3 * (size_t)set->T * sizeof(double), st);
+  double* pool = (double*)pool_t.ptr;
+  cufftDoubleComplex* spec = (cufftDoubleComplex*)spec_t.ptr;
+  double* s1 = (double*)s1_t.ptr;
   double* s2 = s1 + set->T;
   double* s3 = s2 + set->T;
   BSK_CHECK_CUDA(cudaMemsetAsync(ntri, 0, (size_t)set->T * sizeof(double), st));
@@ -598,9 +640,9 @@ void gridinfo_stream(bsk_plan* p, const bsk_triset* set, double* ntri, double* k
   }
   for (double* o : {ntri, s1, s2, s3}) copy_dups(set, o, st);
   launch_gridinfo_finish(set->T, 1.0 / (double)p->K, ntri, s1, s2, s3, kmean, st);
-  BSK_CHECK_CUDA(cudaFreeAsync(s1, st));
-  BSK_CHECK_CUDA(cudaFreeAsync(spec, st));
-  BSK_CHECK_CUDA(cudaFreeAsync(pool, st));
+  s1_t.release();
+  spec_t.release();
+  pool_t.release();
   p->last_stream_C = C;
 }
 
@@ -637,7 +679,8 @@ int bsk_plan_create(int nmesh, double box_size, int n_shells, const double* shel
     BSK_REQUIRE(shell_edges, BSK_ERR_ARG, "shell_edges is NULL");
     BSK_REQUIRE(grid_mode == BSK_GRID_REDUCED || grid_mode == BSK_GRID_NATIVE, BSK_ERR_ARG,
                 "bad grid mode");
-    std::unique_ptr<bsk_plan> p(new bsk_plan());
+    // an error before the plan is handed out releases what it holds so far
+    std::unique_ptr<bsk_plan, void (*)(bsk_plan*)> p(new bsk_plan(), destroy_plan);
     BSK_CHECK_CUDA(cudaGetDevice(&p->device));
     BSK_CHECK_CUDA(cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount,
                                           p->device));
@@ -665,18 +708,20 @@ int bsk_plan_create(int nmesh, double box_size, int n_shells, const double* shel
     p->d_edges = (double*)dmalloc((size_t)2 * n_shells * sizeof(double));
     BSK_CHECK_CUDA(cudaMemcpy(p->d_edges, p->edges.data(), 2 * n_shells * sizeof(double),
                               cudaMemcpyHostToDevice));
-    unsigned long long* d_counts = (unsigned long long*)dmalloc(n_shells * sizeof(unsigned long long));
-    int* d_flag = (int*)dmalloc(2 * sizeof(int));
-    BSK_CHECK_CUDA(cudaMemset(d_counts, 0, n_shells * sizeof(unsigned long long)));
-    BSK_CHECK_CUDA(cudaMemset(d_flag, 0, 2 * sizeof(int)));
-    launch_shell_table(p.get(), d_counts, d_flag, 0);
     std::vector<unsigned long long> hc(n_shells);
     int hf[2] = {0, 0};
-    BSK_CHECK_CUDA(cudaMemcpy(hc.data(), d_counts, n_shells * sizeof(unsigned long long),
-                              cudaMemcpyDeviceToHost));
-    BSK_CHECK_CUDA(cudaMemcpy(hf, d_flag, 2 * sizeof(int), cudaMemcpyDeviceToHost));
-    cudaFree(d_counts);
-    cudaFree(d_flag);
+    {
+      SyncTemp counts_t(n_shells * sizeof(unsigned long long));
+      SyncTemp flag_t(2 * sizeof(int));
+      unsigned long long* d_counts = (unsigned long long*)counts_t.ptr;
+      int* d_flag = (int*)flag_t.ptr;
+      BSK_CHECK_CUDA(cudaMemset(d_counts, 0, n_shells * sizeof(unsigned long long)));
+      BSK_CHECK_CUDA(cudaMemset(d_flag, 0, 2 * sizeof(int)));
+      launch_shell_table(p.get(), d_counts, d_flag, 0);
+      BSK_CHECK_CUDA(cudaMemcpy(hc.data(), d_counts, n_shells * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost));
+      BSK_CHECK_CUDA(cudaMemcpy(hf, d_flag, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+    }  // both freed here (or by an error unwinding the block)
     BSK_REQUIRE(hf[0] == 0, BSK_ERR_UNSUPPORTED,
                 "a Fourier mode lies in shells that are not consecutive; give shells sorted "
                 "by edge with overlaps only between neighbours");
@@ -732,7 +777,8 @@ int bsk_triset_create(bsk_plan* p, int64_t n_tri, const int32_t* tri, bsk_triset
     BSK_REQUIRE(n_tri < (1ll << 31), BSK_ERR_UNSUPPORTED, "too many triangles");
     *out = nullptr;
     DeviceGuard g(p->device);
-    std::unique_ptr<bsk_triset> s(new bsk_triset());
+    // an error before the set is handed out releases what it holds so far
+    std::unique_ptr<bsk_triset, void (*)(bsk_triset*)> s(new bsk_triset(), destroy_triset);
     s->plan = p;
     s->T = n_tri;
     std::map<std::tuple<int, int, int>, int> first;
@@ -774,15 +820,7 @@ int bsk_triset_create(bsk_plan* p, int64_t n_tri, const int32_t* tri, bsk_triset
 }
 
 int bsk_triset_destroy(bsk_triset* set) {
-  return guarded([&] {
-    if (!set) return;
-    DeviceGuard g(set->plan->device);
-    set->sched.release();
-    for (auto& kv : set->groups)
-      for (auto& g : kv.second) g.sched.release();
-    if (set->dups) cudaFree(set->dups);
-    delete set;
-  });
+  return guarded([&] { destroy_triset(set); });
 }
 
 int64_t bsk_triset_size(const bsk_triset* set) { return set ? set->T : -1; }
@@ -851,12 +889,13 @@ void paint(bsk_plan* p, int slot, const float* mesh, int nmesh_cic, cudaStream_t
   if (nfull) make_r2c_sub(p, nfull);
   cufftHandle h = nfull ? p->r2c_sub : p->r2c;
   size_t fine_elems = (size_t)p->N * p->N * (p->N / 2 + 1);
-  cufftComplex* fine = (cufftComplex*)dmalloc_async(fine_elems * sizeof(cufftComplex), st);
+  AsyncTemp fine_t(fine_elems * sizeof(cufftComplex), st);
+  cufftComplex* fine = (cufftComplex*)fine_t.ptr;
   bind_work(p, h, st);
   BSK_CHECK_CUFFT(cufftExecR2C(h, const_cast<float*>(mesh), fine));
   if (!f.spec) f.spec = (cufftComplex*)dmalloc((size_t)p->Mh * sizeof(cufftComplex));
   launch_extract(p, fine, f.spec, axis_w, st);
-  BSK_CHECK_CUDA(cudaFreeAsync(fine, st));
+  fine_t.release();
   f.painted = true;
   ++f.gen;
   f.fields_ok = false;
@@ -979,13 +1018,15 @@ int bsk_contract(bsk_plan* p, const bsk_triset* set, const float* f1, const floa
     cudaStream_t st = (cudaStream_t)stream;
     if (set->T == 0) return;  // nothing to write: out may be NULL
     BSK_REQUIRE(out, BSK_ERR_ARG, "NULL argument");
+    std::unique_ptr<AsyncTemp> split_t;
     __nv_bfloat16* split = nullptr;
     if (precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16) {
-      split = (__nv_bfloat16*)dmalloc_async(split_elems(p->n, K) * sizeof(__nv_bfloat16), st);
+      split_t.reset(new AsyncTemp(split_elems(p->n, K) * sizeof(__nv_bfloat16), st));
+      split = (__nv_bfloat16*)split_t->ptr;
       launch_split(f3, p->n, K, split, st);
     }
     contract_dispatch(p, set, f1, f2, f3, split, p->n, K, 0, K, precision, out, st);
-    if (split) BSK_CHECK_CUDA(cudaFreeAsync(split, st));
+    if (split_t) split_t->release();
   });
 }
 
@@ -1008,10 +1049,12 @@ int bsk_gridinfo(bsk_plan* p, const bsk_triset* set, double* ntri, double* kmean
       return;
     }
     p->last_stream_C = 0;
-    double* nf = (double*)dmalloc_async(fbytes, st);
-    double* kf = (double*)dmalloc_async(fbytes, st);
-    cufftDoubleComplex* spec = (cufftDoubleComplex*)dmalloc_async(
-        (size_t)p->chunk * p->Mh * sizeof(cufftDoubleComplex), st);
+    AsyncTemp nf_t(fbytes, st);
+    AsyncTemp kf_t(fbytes, st);
+    double* nf = (double*)nf_t.ptr;
+    double* kf = (double*)kf_t.ptr;
+    AsyncTemp spec_t((size_t)p->chunk * p->Mh * sizeof(cufftDoubleComplex), st);
+    cufftDoubleComplex* spec = (cufftDoubleComplex*)spec_t.ptr;
     for (int kw = 0; kw < 2; ++kw) {
       double* dst = kw ? kf : nf;
       for (int s0 = 0; s0 < p->n; s0 += p->chunk) {
@@ -1024,8 +1067,9 @@ int bsk_gridinfo(bsk_plan* p, const bsk_triset* set, double* ntri, double* kmean
         BSK_CHECK_CUFFT(cufftExecZ2D(p->z2d, spec, dst + (size_t)s0 * p->K));
       }
     }
-    BSK_CHECK_CUDA(cudaFreeAsync(spec, st));
-    double* s1 = (double*)dmalloc_async((size_t)3 * set->T * sizeof(double), st);
+    spec_t.release();
+    AsyncTemp s1_t((size_t)3 * set->T * sizeof(double), st);
+    double* s1 = (double*)s1_t.ptr;
     double* s2 = s1 + set->T;
     double* s3 = s2 + set->T;
     auto run = [&](const double* a, const double* b, const double* c, double* o) {
@@ -1038,9 +1082,9 @@ int bsk_gridinfo(bsk_plan* p, const bsk_triset* set, double* ntri, double* kmean
     run(nf, kf, nf, s2);
     run(nf, nf, kf, s3);
     launch_gridinfo_finish(set->T, 1.0 / (double)p->K, ntri, s1, s2, s3, kmean, st);
-    BSK_CHECK_CUDA(cudaFreeAsync(s1, st));
-    BSK_CHECK_CUDA(cudaFreeAsync(nf, st));
-    BSK_CHECK_CUDA(cudaFreeAsync(kf, st));
+    s1_t.release();
+    nf_t.release();
+    kf_t.release();
   });
 }
 
