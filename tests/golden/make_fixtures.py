@@ -195,6 +195,12 @@ def main(ref_root):
         rows = [next(f) for _ in range(12)]
     with open(os.path.join(HERE, "ps_modes_512_head.dat"), "w") as f:
         f.writelines(rows)
+    # the N_modes column of every row: shells [i + 0.5, i + 1.5] kf, i = 0..254, at 512^3
+    pk = np.loadtxt(os.path.join(src, "test_grid_512_1_ps_kf_0.5kf.dat"))
+    with open(os.path.join(HERE, "ps_nmodes_512.dat"), "w") as f:
+        f.write("# N_modes of shells [i + 0.5, i + 1.5] k_f, i = 0..%d, Nmesh 512, L 1000 "
+                "(test_grid_512_1_ps_kf_0.5kf.dat, third column)\n" % (len(pk) - 1))
+        f.writelines("%d\n" % int(round(v)) for v in pk[:, 2])
 
 
 if __name__ == "__main__":

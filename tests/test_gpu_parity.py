@@ -14,6 +14,8 @@ Tolerances (stated per test):
   no longer a 1e-5 relative one), and a median rel <= 1e-5 over all bins;
   bf16 (one MMA term) must meet nrm <= 1e-3.
 """
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -75,6 +77,18 @@ def test_mode_counts_exact(cuda, grid):
     plan = Plan(512, 1000.0, edges, grid="reduced")
     assert plan.ngrid < 512
     assert plan.mode_counts().tolist() == [18, 62, 98, 210]
+
+
+def test_mode_counts_match_all_golden_pk_rows(cuda):
+    # all 255 rows of bskit's P(k) golden file (shells [i + 0.5, i + 1.5] k_f at 512^3,
+    # L = 1000, up to the Nyquist corner): the plan's exact counts on the full grid
+    gold = np.loadtxt(os.path.join(os.path.dirname(__file__), "golden",
+                                   "ps_nmodes_512.dat")).astype(np.int64)
+    kf = TWO_PI / 1000.0
+    edges = np.array([[0.5 + i, 1.5 + i] for i in range(len(gold))]) * kf
+    plan = Plan(512, 1000.0, edges, grid="native")
+    assert np.array_equal(plan.mode_counts(), gold)
+    plan.close()
 
 
 def test_gridinfo_matches_golden_text(cuda):

@@ -66,6 +66,16 @@ def test_mode_counts_match_golden_pk():
     assert np.array_equal(counts, gold[:, 2].astype(np.int64))
 
 
+def test_mode_counts_match_all_golden_pk_rows_inside_the_grid():
+    # every shell of radius below 63.5 k_f has the same count on a 128^3 grid as on the
+    # golden file's 512^3 one: the first 62 of its 255 rows pin the oracle's predicate
+    gold = np.loadtxt(os.path.join(GOLD, "ps_nmodes_512.dat")).astype(np.int64)
+    assert len(gold) == 255
+    kf = 2 * np.pi / 1000.0
+    edges = np.array([[0.5 + i, 1.5 + i] for i in range(62)]) * kf
+    assert np.array_equal(O.shell_mode_counts(128, 1000.0, edges), gold[:62])
+
+
 def test_mode_counts_equal_parseval_definition():
     n, box = 16, 100.0
     kf = 2 * np.pi / box
