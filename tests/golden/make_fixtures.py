@@ -201,6 +201,17 @@ def main(ref_root):
         f.write("# N_modes of shells [i + 0.5, i + 1.5] k_f, i = 0..%d, Nmesh 512, L 1000 "
                 "(test_grid_512_1_ps_kf_0.5kf.dat, third column)\n" % (len(pk) - 1))
         f.writelines("%d\n" % int(round(v)) for v in pk[:, 2])
+    # they are the exact closed-shell counts of the full 512^3 grid: |q|^2 is an integer, so
+    # [n - 1/2, n + 1/2] k_f holds the modes with n^2 - n + 1 <= |q|^2 <= n^2 + n
+    q = np.fft.fftfreq(512, 1.0 / 512).astype(np.int64)
+    r2max = 3 * 256 ** 2
+    yz = np.bincount((q[:, None] ** 2 + q[None, :] ** 2).ravel(), minlength=r2max + 1)
+    hist = np.zeros(r2max + 1, dtype=np.int64)
+    for qx in q:
+        hist[qx * qx:] += yz[:r2max + 1 - qx * qx]
+    cum = np.concatenate([[0], np.cumsum(hist)])
+    exact = [cum[n * n + n + 1] - cum[n * n - n + 1] for n in range(1, len(pk) + 1)]
+    assert np.array_equal(np.array(exact), np.rint(pk[:, 2]).astype(np.int64))
 
 
 if __name__ == "__main__":
