@@ -82,3 +82,30 @@ def test_host_checks_reject_bad_buffers():
         engine._check_tensor(good, "out", (5,), torch.float64, torch.device("cuda", 0))
     with pytest.raises(ValueError):
         engine.Plan.normalize(good, good)  # host tensors
+
+
+def test_noalloc_arguments_rejected_without_gpu(lib):
+    # checks that run before any CUDA call
+    tri = (ctypes.c_int32 * 3)(0, 0, 0)
+    f = ctypes.c_void_p(16)  # never dereferenced: every call below fails its checks first
+    out = ctypes.c_void_p(16)
+    P = _lib.PREC_BF16X3
+    cases = [
+        (0, 1, tri, f, 1024, P, out),        # no shells
+        (256, 1, tri, f, 1024, P, out),      # more shells than a plan allows
+        (1, 1, None, f, 1024, P, out),       # triangles missing
+        (1, -1, tri, f, 1024, P, out),       # negative count
+        (1, 1, tri, None, 1024, P, out),     # field missing
+        (1, 1, tri, f, 1004, P, out),        # k_points not a multiple of 8
+        (1, 1, tri, f, 1024, _lib.PREC_FP64, out),  # SIMT precisions are not offered here
+    ]
+    for n, t, tr, ff, k, prec, o in cases:
+        rc = lib.bsk_contract_noalloc(n, t, tr, ff, ff if ff else f, ff if ff else f, k, prec,
+                                      o, None)
+        assert rc == _lib.BSK_ERR_ARG, (n, t, k, prec, _lib.last_error())
+    # an empty list is a valid request that does nothing
+    assert lib.bsk_contract_noalloc(1, 0, None, f, f, f, 1024, P, None, None) == _lib.BSK_OK
+    # the plan-based entry points reject a missing plan before touching the device
+    assert lib.bsk_measure_b(None, None, 0, 0, 0, P, None, None) == _lib.BSK_ERR_ARG
+    assert lib.bsk_gridinfo(None, None, None, None, None) == _lib.BSK_ERR_ARG
+    assert lib.bsk_contract(None, None, f, f, f, 1024, P, out, None) == _lib.BSK_ERR_ARG
