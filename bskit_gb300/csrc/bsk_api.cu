@@ -1009,6 +1009,8 @@ int bsk_contract(bsk_plan* p, const bsk_triset* set, const float* f1, const floa
                  const float* f3, int64_t K, int precision, double* out, void* stream) {
   return guarded([&] {
     BSK_REQUIRE(p && set && f1 && f2 && f3, BSK_ERR_ARG, "NULL argument");
+    BSK_REQUIRE(((uintptr_t)f1 | (uintptr_t)f2 | (uintptr_t)f3) % 16 == 0, BSK_ERR_ARG,
+                "field pointers must be 16-byte aligned");
     BSK_REQUIRE(set->plan == p, BSK_ERR_ARG, "triangle set belongs to another plan");
     BSK_REQUIRE(K > 0 && K % 8 == 0, BSK_ERR_ARG, "k_points must be a positive multiple of 8");
     BSK_REQUIRE(precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16 ||

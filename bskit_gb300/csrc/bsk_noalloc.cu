@@ -13,15 +13,25 @@
 //
 // Properties callers rely on:
 //  * the array is part of this library's device image: every GPU that loads
-//    the library holds it until the process exits;
+//    the library holds it until the process exits.  With CUDA's lazy module
+//    loading the array is committed when the library's device code is first
+//    loaded on a device, which may be this entry point's first call: make one
+//    warm-up call on each device before reserving the rest of its memory;
 //  * the first call on a device resolves the array's device address with
-//    cudaGetSymbolAddress (once per device, with that device current); make
-//    that first call before any stream capture;
+//    cudaGetSymbolAddress (once per device, with that device current);
+//  * every call synchronises `stream`: the schedule is copied from pageable
+//    host memory, and the call waits for those copies before it returns.  A
+//    call made while `stream` is being captured into a CUDA graph is rejected
+//    with BSK_ERR_STATE before it enqueues anything;
+//  * any CUDA error still pending on the calling thread from earlier work is
+//    consumed (cleared) once the arguments have passed their checks;
 //  * every call shares the array and it keeps the last call's contents; each
 //    call rewrites everything it later reads (and zeroes the output), so no
 //    result depends on an earlier call -- but two calls whose work overlaps on
 //    the GPU (different streams, no ordering) race on the array;
-//  * requests that do not fit in the array are rejected with BSK_ERR_ARG.
+//  * requests that do not fit in the array are rejected with BSK_ERR_ARG, and
+//    so are field pointers that are not 16-byte aligned (the kernels read
+//    them with 16-byte vector loads and TMA).
 #include <algorithm>
 #include <mutex>
 #include <set>
@@ -47,8 +57,10 @@ void* scratch_address(int dev) {
     cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
     if (e != cudaSuccess) {
       cudaGetLastError();
-      throw Error{BSK_ERR_CUDA, std::string("cudaGetSymbolAddress(static scratch): ") +
-                                    cudaGetErrorString(e)};
+      // the array is committed when the module loads: no room for it is an out-of-memory
+      throw Error{e == cudaErrorMemoryAllocation ? BSK_ERR_OOM : BSK_ERR_CUDA,
+                  std::string("cudaGetSymbolAddress(static scratch): ") +
+                      cudaGetErrorString(e)};
     }
     g_scratch_ptr[dev] = p;
   }
@@ -82,17 +94,26 @@ using namespace bsk;
 extern "C" int bsk_contract_noalloc(int n_shells, int64_t n_tri, const int32_t* tri,
                                     const float* f1, const float* f2, const float* f3,
                                     int64_t k_points, int precision, double* out, void* stream) {
-  cudaGetLastError();
   try {
     BSK_REQUIRE(n_shells >= 1 && n_shells <= 255, BSK_ERR_ARG, "need 1..255 shells");
     BSK_REQUIRE(n_tri >= 0 && (n_tri == 0 || (tri && out)), BSK_ERR_ARG, "bad triangle list");
     BSK_REQUIRE(f1 && f2 && f3, BSK_ERR_ARG, "NULL field pointer");
+    BSK_REQUIRE(((uintptr_t)f1 | (uintptr_t)f2 | (uintptr_t)f3) % 16 == 0, BSK_ERR_ARG,
+                "field pointers must be 16-byte aligned");
     BSK_REQUIRE(k_points > 0 && k_points % 8 == 0, BSK_ERR_ARG,
                 "k_points must be a positive multiple of 8");
     BSK_REQUIRE(precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16, BSK_ERR_ARG,
                 "the allocation-free contraction runs the tensor-core precisions (bf16x3, bf16)");
+    BSK_REQUIRE(((uintptr_t)out) % 8 == 0, BSK_ERR_ARG, "output pointer must be 8-byte aligned");
     if (n_tri == 0) return BSK_OK;
     cudaStream_t st = (cudaStream_t)stream;
+    // the call synchronises its stream (pageable copies + wait below), which a capture forbids
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    BSK_CHECK_CUDA(cudaStreamIsCapturing(st, &cap));
+    BSK_REQUIRE(cap == cudaStreamCaptureStatusNone, BSK_ERR_STATE,
+                "bsk_contract_noalloc synchronises its stream and cannot be captured into a "
+                "CUDA graph; call it outside stream capture");
+    cudaGetLastError();  // a stale error of earlier work must not be reported as this call's
     int dev = 0;
     BSK_CHECK_CUDA(cudaGetDevice(&dev));
     int num_sms = 0;

@@ -15,7 +15,9 @@
  *    caller-owned device buffers of float64.
  *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
  *    Work is enqueued on that stream; the host does not synchronise except
- *    in bsk_plan_create / bsk_triset_create / bsk_shell_mode_counts.
+ *    in bsk_plan_create / bsk_triset_create / bsk_shell_mode_counts /
+ *    bsk_compensate_cic / bsk_sync_check / bsk_contract_noalloc (which waits
+ *    for its own schedule copies on `stream` and so cannot be captured).
  *  - A plan is bound to the CUDA device that was current at creation.
  *    Calls on one plan must be serialised by the caller; distinct plans may
  *    run on distinct streams concurrently.
@@ -214,8 +216,9 @@ int bsk_gridinfo(bsk_plan* plan, const bsk_triset* set, double* ntri, double* km
 int bsk_normalize(int64_t n, const double* b_unnorm, const double* ntri, double* b_out, void* stream);
 
 /*
- * Contract caller-provided real-space fields (device, float32 [n][K]) for a
- * triangle set: out[t] = sum_k f1[i_t][k] f2[j_t][k] f3[l_t][k]  (no scale).
+ * Contract caller-provided real-space fields (device, float32 [n][K], each
+ * 16-byte aligned) for a triangle set:
+ *   out[t] = sum_k f1[i_t][k] f2[j_t][k] f3[l_t][k]  (no scale).
  * Used by the precision study and the kernel tests; bsk_measure_b calls the
  * same kernels on the plan's own fields.
  * Replaces: the per-triangle np.sum(I_a*I_b*I_c), bskit/main.py:1875.
@@ -243,15 +246,21 @@ int bsk_sync_check(void* stream);
  * Allocation-free variant of bsk_contract for the tensor-core precisions
  * (BSK_PREC_BF16X3, BSK_PREC_BF16): out[t] = sum_k f1[i_t][k] f2[j_t][k] f3[l_t][k]
  * for n_tri host triangles (int32 [T][3] shell indices, no repeats) over
- * device fields [n_shells][k_points].  No counterpart in the reference: it
- * serves callers that cannot call cudaMalloc -- a process whose framework
- * reserved the device memory up front, or a pipeline that forbids
+ * device fields [n_shells][k_points] (16-byte aligned).  No counterpart in the
+ * reference: it serves callers that cannot call cudaMalloc -- a process whose
+ * framework reserved the device memory up front, or a pipeline that forbids
  * cudaMalloc/cudaFree (which synchronise and can fail) on its hot path.
  * All scratch (the contraction schedule and the bf16 split of f3) lives in one
  * 64 MiB static device array of the library, held by every GPU that loads the
  * library until exit; a request needing more (about n_shells * k_points * 4
- * bytes plus the schedule) is rejected with BSK_ERR_ARG.  The first call on a
- * device looks up the array's address (make it before any stream capture).
+ * bytes plus the schedule) is rejected with BSK_ERR_ARG.  The array may only be
+ * committed when the library's device code first loads on a device: make one
+ * warm-up call per device before reserving the rest of its memory (no room for
+ * the array is reported as BSK_ERR_OOM).  The first call on a device also looks
+ * up the array's address.  Every call synchronises `stream` (it copies the
+ * schedule from host memory and waits for the copies); a call on a stream that
+ * is being captured is rejected with BSK_ERR_STATE.  A CUDA error pending on the
+ * calling thread from earlier work is consumed once the arguments are checked.
  * Calls share the array: each rewrites what it reads, but calls whose work
  * overlaps on the GPU race.  No plan or triangle set is needed.
  */

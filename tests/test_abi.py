@@ -98,6 +98,7 @@ def test_noalloc_arguments_rejected_without_gpu(lib):
         (1, 1, tri, None, 1024, P, out),     # field missing
         (1, 1, tri, f, 1004, P, out),        # k_points not a multiple of 8
         (1, 1, tri, f, 1024, _lib.PREC_FP64, out),  # SIMT precisions are not offered here
+        (1, 1, tri, ctypes.c_void_p(20), 1024, P, out),  # field not 16-byte aligned
     ]
     for n, t, tr, ff, k, prec, o in cases:
         rc = lib.bsk_contract_noalloc(n, t, tr, ff, ff if ff else f, ff if ff else f, k, prec,
@@ -109,3 +110,6 @@ def test_noalloc_arguments_rejected_without_gpu(lib):
     assert lib.bsk_measure_b(None, None, 0, 0, 0, P, None, None) == _lib.BSK_ERR_ARG
     assert lib.bsk_gridinfo(None, None, None, None, None) == _lib.BSK_ERR_ARG
     assert lib.bsk_contract(None, None, f, f, f, 1024, P, out, None) == _lib.BSK_ERR_ARG
+    # a misaligned output pointer is rejected before the capture check or any device call
+    assert lib.bsk_contract_noalloc(1, 1, tri, f, f, f, 1024, P, ctypes.c_void_p(20),
+                                    None) == _lib.BSK_ERR_ARG
