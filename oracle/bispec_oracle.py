@@ -138,6 +138,68 @@ def triple_sums(fa, fb, fc, tri):
     return out
 
 
+def _irfftn3(spec, n, workers):
+    """Unnormalised c2r through scipy.fft with host threads when available (same
+    transform as ``c2r``; used for the large grids of the configuration tests)."""
+    try:
+        import scipy.fft as sf
+        return sf.irfftn(spec, s=(n, n, n), axes=(0, 1, 2), workers=workers) * float(n) ** 3
+    except ImportError:
+        return c2r(spec, n)
+
+
+def shell_fields_subset(dhat, n, box, shell_edges, shells, workers=-1):
+    """I_i(x) (float64) of the listed shells only, as a dict shell -> (n, n, n) array.
+
+    Same definition as ``shell_fields`` (masked pmesh c2r, main.py:1846-1861); for
+    large grids where only the shells of a sample of triangle bins are needed."""
+    kk = mode_kk(n, box)
+    out = {}
+    for s in sorted(set(int(v) for v in shells)):
+        lo, hi = shell_edges[s]
+        out[s] = _irfftn3(dhat * shell_mask(kk, lo, hi), n, workers)
+    return out
+
+
+def triple_sums_blocked(fa, fb, fc, tri, block=8, workers=None):
+    """(S, A): S[t] = sum_x fa[i_t] fb[j_t] fc[l_t] and A[t] = sum_x |fa fb fc|, float64.
+
+    fa / fb / fc map a shell index to its (n, n, n) field (arrays or dicts).  The
+    sum over x runs in blocks of ``block`` x-planes on a pool of host threads
+    (numpy releases the GIL), each block reusing its pair products for every third
+    shell; the block partial sums are added in float64 (main.py:1875 sums the
+    product over the whole grid; only the summation order differs)."""
+    import concurrent.futures as cf
+    import os
+
+    tri = np.asarray(tri, dtype=np.int64).reshape(-1, 3)
+    pairs = {}
+    for t, (i, j, l) in enumerate(tri):
+        pairs.setdefault((int(i), int(j)), []).append((t, int(l)))
+    n = next(iter(fa.values())).shape[0] if isinstance(fa, dict) else fa.shape[1]
+
+    def one(x0):
+        x1 = min(n, x0 + block)
+        S = np.zeros(len(tri))
+        A = np.zeros(len(tri))
+        for (i, j), items in pairs.items():
+            p = (fa[i][x0:x1] * fb[j][x0:x1]).ravel()
+            ap = np.abs(p)
+            for t, l in items:
+                c = fc[l][x0:x1].ravel()
+                S[t] += p @ c
+                A[t] += ap @ np.abs(c)
+        return S, A
+
+    S = np.zeros(len(tri))
+    A = np.zeros(len(tri))
+    with cf.ThreadPoolExecutor(max_workers=workers or os.cpu_count() or 4) as ex:
+        for s_, a_ in ex.map(one, range(0, n, block)):
+            S += s_
+            A += a_
+    return S, A
+
+
 def bispectrum_unnormalized(meshes, box, shell_edges, tri, pos_units=1.0):
     """B_unnorm for every triangle (the ``measure_bispectrum_faster`` output).
 
