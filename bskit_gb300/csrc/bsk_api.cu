@@ -1041,6 +1041,11 @@ int bsk_gridinfo(bsk_plan* p, const bsk_triset* set, double* ntri, double* kmean
     cudaStream_t st = (cudaStream_t)stream;
     if (set->T == 0) return;  // nothing to write: ntri and kmean may be NULL
     BSK_REQUIRE(ntri && kmean, BSK_ERR_ARG, "NULL argument");
+    if (gridinfo_enum_supported(p)) {  // exact integer enumeration, no FFT
+      p->last_stream_C = 0;
+      gridinfo_enum(p, set->tri, ntri, kmean, st);
+      return;
+    }
     make_z2d(p);
     bind_work(p, p->z2d, st);
     const size_t fbytes = (size_t)p->n_alloc() * p->K * sizeof(double);

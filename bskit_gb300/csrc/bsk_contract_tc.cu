@@ -11,7 +11,7 @@
 //     per 64-point K block an operand of nc hi rows followed by nc lo rows;
 //     SWIZZLE_128B, K-major), and the FP32 tile(s) of the pair-factor shells
 //     (one tile when one range covers both factors of every row, as for auto
-//     spectra), each with only as many shell rows (16/32/48/64) as the tile uses.
+//     spectra), each with only as many shell rows (a multiple of 8) as the tile uses.
 //     A stage's source tiles are refilled as soon as the A-operand warps have read
 //     them and its B tiles once the stage's MMAs completed, each part with its own
 //     "landed" barrier, so the sources get about one more stage of lead time;
@@ -23,7 +23,9 @@
 //   * warp 1 runs the stage loop and one elected lane issues, per 16-point K step,
 //     tcgen05.mma kind::f16 with A from TMEM and B from SMEM: hi x [Bhi; Blo]
 //     (N = 2 nc: one MMA yields both hi*Bhi and hi*Blo) and, for bf16x3, lo x Bhi
-//     (N = nc, into the hi*Bhi columns).  The tensor core's FP32 accumulate
+//     (N = nc rounded up to the MMA's multiple of 16, into the hi*Bhi columns; when
+//     nc is an odd multiple of 8 the last 8 of those N columns are lo x Blo of the
+//     first 8 column shells, landing on their hi*Blo sums: an extra, exact term).  The tensor core's FP32 accumulate
 //     truncates, so an accumulator is only ever fed one stage (16 MMAs) before it is
 //     handed over;
 //   * warps 2..9 (2 per lane quadrant, 32 columns each) drain each finished
@@ -106,13 +108,16 @@ constexpr int smem_bytes() {
 
 // Tensor maps of one launch.  B: a 5D view of the chunk-major bf16 split {64 points,
 // shell, hi/lo plane, 64-point block, 128-point chunk} with box {64, nc, 2, 2, 1}: one
-// contiguous copy per stage.  Sources: FP32 [shell][K] with 16/32/64-row boxes (2D, one
-// 32-point block per copy) and, when the grid is a multiple of 128 points, the one-copy
-// view {32 points, shell, 32-point block} with box {32, rows, 4}.
+// contiguous copy per stage, one map per nc = 8, 16, ..., 64.  Sources: FP32 [shell][K]
+// with 16/32/64-row boxes (2D, one 32-point block per copy) and, when the grid is a
+// multiple of 128 points, the one-copy view {32 points, shell, 32-point block} with box
+// {32, rows, 4}, one map per rows = 8, 16, ..., 64.
+constexpr int kRowSizes = kMaxCols / 8;
 struct Maps {
   CUtensorMap f1_16, f1_32, f1_64, f2_16, f2_32, f2_64;
-  CUtensorMap b16, b32, b48, b64, a1_16, a1_32, a1_48, a1_64, a2_16, a2_32, a2_48, a2_64;
+  CUtensorMap b[kRowSizes], a1[kRowSizes], a2[kRowSizes];
 };
+static_assert(kMaxSrcRows == kMaxCols, "one row-size list serves B and the sources");
 
 __device__ int g_tc_error;  // 0 ok, 1 a bounded wait expired
 
@@ -209,11 +214,10 @@ __device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map
       "r"(smem_u32(bar))
       : "memory");
 }
-__device__ __forceinline__ const CUtensorMap* by_rows(int n, const CUtensorMap* m16,
-                                                      const CUtensorMap* m32,
-                                                      const CUtensorMap* m48,
-                                                      const CUtensorMap* m64) {
-  return n > 48 ? m64 : n > 32 ? m48 : n > 16 ? m32 : m16;
+// The map of a list for a row count n (a multiple of 8, 8..64).
+__device__ __forceinline__ const CUtensorMap* by_rows(const CUtensorMap (&maps)[kRowSizes],
+                                                      int n) {
+  return &maps[(n >> 3) - 1];
 }
 // One lane of a fully active warp (elect.sync picks the lowest active lane).
 __device__ __forceinline__ bool elect_one() {
@@ -394,8 +398,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         // bytes per stage: the four 32-point quarters of each source tile; the column rows
         // of hi and lo in both K blocks
         const uint32_t src_bytes =
-            (uint32_t)(4 * 128 * (box_rows(td.ni) + (one_src ? 0 : box_rows(td.nj))));
-        const uint32_t b_bytes = (uint32_t)(4 * box_rows(td.nc) * 128);
+            fused ? (uint32_t)(4 * 128 * (td.ni + (one_src ? 0 : td.nj)))
+                  : (uint32_t)(4 * 128 * (box_rows(td.ni) + (one_src ? 0 : box_rows(td.nj))));
+        const uint32_t b_bytes = (uint32_t)(4 * td.nc * 128);
         for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
           const int s = chunk % SST;
           const uint32_t st = sbase + s * STAGE_BYTES;
@@ -411,12 +416,10 @@ __global__ void __launch_bounds__(THREADS, 1)
           mbar_arrive_tx(&bars->full[s], src_bytes);
           if (fused) {
             // one copy per source tile ([32-point block][rows])
-            tma_load_3d(st + 2 * B_BLOCK,
-                        by_rows(td.ni, &maps.a1_16, &maps.a1_32, &maps.a1_48, &maps.a1_64),
-                        &bars->full[s], 0, td.i0, xi / 32);
+            tma_load_3d(st + 2 * B_BLOCK, by_rows(maps.a1, td.ni), &bars->full[s], 0, td.i0,
+                        xi / 32);
             if (!one_src)
-              tma_load_3d(st + 2 * B_BLOCK + 4 * 128 * box_rows(td.ni),
-                          by_rows(td.nj, &maps.a2_16, &maps.a2_32, &maps.a2_48, &maps.a2_64),
+              tma_load_3d(st + 2 * B_BLOCK + 4 * 128 * td.ni, by_rows(maps.a2, td.nj),
                           &bars->full[s], 0, td.j0, xi / 32);
           } else {
             for (int q = 0; q < 4; ++q) {
@@ -435,8 +438,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           mbar_arrive_tx(&bars->full_b[s], b_bytes);
           // one contiguous copy for B: the stage's 128-point chunk of the split, nc shells,
           // both planes, both 64-point blocks -> [block][plane][nc rows][64]
-          tma_load_5d(st, by_rows(td.nc, &maps.b16, &maps.b32, &maps.b48, &maps.b64),
-                      &bars->full_b[s], 0, td.l0, 0, 0, xi / KCH);
+          tma_load_5d(st, by_rows(maps.b, td.nc), &bars->full_b[s], 0, td.l0, 0, 0, xi / KCH);
         }
       }
     }
@@ -452,11 +454,13 @@ __global__ void __launch_bounds__(THREADS, 1)
       const TileDesc td = tiles[item % n_tiles];
       const int64_t x_begin = k_begin + sl * slice;
       const int64_t x_end = min(k_end, x_begin + slice);
-      // hi x [Bhi; Blo] (the lo rows of a block sit right after its nc hi rows), lo x Bhi
-      const int lo_row = td.nc;
+      // hi x [Bhi; Blo] (the lo rows of a block sit right after its nc hi rows), lo x Bhi.
+      // N is a multiple of 16: an N = nc MMA with nc an odd multiple of 8 also covers the
+      // first 8 lo rows (accumulated into hi*Blo columns the drain adds anyway, or never read)
+      const int n16 = (td.nc + 15) & ~15;
       const uint32_t kb_bytes = 2u * td.nc * 128u;
-      const uint32_t idesc_stack = idesc_bf16(terms >= 3 ? lo_row + td.nc : td.nc);
-      const uint32_t idesc_hi = idesc_bf16(td.nc);
+      const uint32_t idesc_stack = idesc_bf16(terms >= 3 ? 2 * td.nc : n16);
+      const uint32_t idesc_hi = idesc_bf16(n16);
       for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
         // a fresh accumulator per stage, once the drain has emptied it
         const uint32_t b = grp % NACC;
@@ -570,9 +574,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int pi = valid ? ri - td.i0 : 0;
       const int pj = valid ? rj - td.j0 : 0;
       // source tiles: [32-point quarter][rows] with the quarter stride of the copy
-      const int qstride = fused ? box_rows(td.ni) * 128 : A_QUARTER;
+      const int qstride = fused ? td.ni * 128 : A_QUARTER;
       const int src2 = one_src ? 0 : (fused ? 4 * qstride : A_TILE);
-      const int qstride2 = one_src ? qstride : (fused ? box_rows(td.nj) * 128 : A_QUARTER);
+      const int qstride2 = one_src ? qstride : (fused ? td.nj * 128 : A_QUARTER);
       for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
         const int s = chunk % SST;
         const uint32_t ph = (chunk / SST) & 1;
@@ -738,16 +742,13 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
   tc::make_map(&m.f2_16, F32, 4, f2, K, n_shells, 32, 16);
   tc::make_map(&m.f2_32, F32, 4, f2, K, n_shells, 32, 32);
   tc::make_map(&m.f2_64, F32, 4, f2, K, n_shells, 32, 64);
-  const int rows16[4] = {16, 32, 48, 64};
-  CUtensorMap* bmaps[4] = {&m.b16, &m.b32, &m.b48, &m.b64};
-  CUtensorMap* a1maps[4] = {&m.a1_16, &m.a1_32, &m.a1_48, &m.a1_64};
-  CUtensorMap* a2maps[4] = {&m.a2_16, &m.a2_32, &m.a2_48, &m.a2_64};
-  for (int i = 0; i < 4; ++i) tc::make_split_map(bmaps[i], f3_split, split_shells, K, rows16[i]);
+  for (int i = 0; i < tc::kRowSizes; ++i)
+    tc::make_split_map(&m.b[i], f3_split, split_shells, K, 8 * (i + 1));
   // one copy per stage per source tile when K is a multiple of the stage
   bool fused = K % tc::KCH == 0;
-  for (int i = 0; i < 4 && fused; ++i) {
-    fused = tc::make_block_map(a1maps[i], F32, 4, f1, K, n_shells, 32, rows16[i], 4) &&
-            tc::make_block_map(a2maps[i], F32, 4, f2, K, n_shells, 32, rows16[i], 4);
+  for (int i = 0; i < tc::kRowSizes && fused; ++i) {
+    fused = tc::make_block_map(&m.a1[i], F32, 4, f1, K, n_shells, 32, 8 * (i + 1), 4) &&
+            tc::make_block_map(&m.a2[i], F32, 4, f2, K, n_shells, 32, 8 * (i + 1), 4);
   }
   bool two_src = f1 != f2;
   for (const TileDesc& d : s.h_tiles) two_src = two_src || d.i0 != d.j0;

@@ -51,7 +51,7 @@ constexpr int kMaxSrcRows = 64; // shells per A-source range (one 64-row TMA box
 
 struct TileDesc {
   int i0, j0, l0;     // first shell of the F1 rows range, F2 rows range, F3 column range
-  int ni, nj, nc;     // extents (nc multiple of 16 <= 64; ni, nj <= 64; i0 == j0 when one
+  int ni, nj, nc;     // extents (multiples of 8: nc <= 64; ni, nj <= 64; i0 == j0 when one
                       // 64-shell range covers both pair factors)
   int nrows;          // valid rows
   int row_off;        // offset of this tile's 128 row entries
@@ -244,6 +244,13 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
 
 // Bounded-wait error flag of the tcgen05 kernel (1 = a wait expired); optionally reset.
 int tc_error_flag(bool reset);
+
+// Grid information by exact lattice enumeration (counts and |k| sums in integers) for
+// plans whose shell modes cannot form a triangle that wraps around the grid and that have
+// at most 64 shells; ntri[T], kmean[T][3] (device).  Synchronises `st`.
+bool gridinfo_enum_supported(const bsk_plan* p);
+void gridinfo_enum(bsk_plan* p, const std::vector<HostTriangle>& tri, double* ntri,
+                   double* kmean, cudaStream_t st);
 
 void launch_scale(double* v, int64_t n, double s, cudaStream_t st);
 void launch_gridinfo_finish(int64_t T, double inv_k, double* ntri, const double* s1,

@@ -52,7 +52,7 @@ def schedule(exe, tmp_path, n, tri):
     # every tile fits the kernel, every triangle is in exactly one entry, at its own place
     seen = np.zeros(len(tri), dtype=int)
     for d in tiles:
-        assert d["nc"] % 16 == 0 and 16 <= d["nc"] <= 64
+        assert d["nc"] % 8 == 0 and 8 <= d["nc"] <= 64
         assert d["ni"] <= 64 and d["nj"] <= 64 and 1 <= d["nrows"] <= 128
         for c in range(d["nc"]):
             for r in range(128):
@@ -75,7 +75,7 @@ def test_headline_schedule(harness, tmp_path):
     tiles = schedule(harness, tmp_path, 63, B.generate_triangle_bin_list(return_indices=True,
                                                                           **kw))
     assert len(tiles) == 9
-    assert sum(d["nrows"] for d in tiles) == 1086 and sum(d["nc"] for d in tiles) == 384
+    assert sum(d["nrows"] for d in tiles) == 1086 and sum(d["nc"] for d in tiles) == 352
 
 
 @pytest.mark.parametrize("num_fields", [2, 3])
