@@ -46,19 +46,23 @@
 namespace bsk {
 namespace genum {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxShells = 64;                     // tables of at most 64 shells
 constexpr int kMaxBatch = 32;                      // octant modes per batch
 constexpr int kFrac = 44;                          // fractional bits of the |q| weights
 constexpr int kLimb = 22;                          // bits of the low limb
 
+// Membership of an integer wavevector in one byte: 0 = no shell, else
+// 0x80 | (count - 1) << 6 | first shell (count 1 or 2, first < 64).
+__host__ __device__ __forceinline__ int code_first(uint32_t c) { return c & 63; }
+__host__ __device__ __forceinline__ int code_last(uint32_t c) { return (c & 63) + ((c >> 6) & 1); }
+
 struct Mode {
   int16_t x, y, z;
-  uint16_t code;         // first shell | (count - 1) << 8, as the plan's table
+  uint16_t code;         // the byte code of the mode
   unsigned long long w;  // |q| * 2^kFrac, rounded (host sqrt, correctly rounded)
 };
-
 static_assert(sizeof(HostTriangle) == 3 * sizeof(int32_t), "triangles upload as int32 [T][3]");
 
 struct Batch {
@@ -76,8 +80,8 @@ __device__ __forceinline__ int isqrt_floor(int t) {
   return s;
 }
 
-// Membership code of the integer wavevector q (all |q_c| < Ng / 2) from the plan's
-// half-complex table: q and -q share it (the predicate squares the components).
+// Plan-table code (first | (count - 1) << 8, 0x00FF none) of the integer wavevector q, all
+// |q_c| < Ng / 2: q and -q share it (the predicate squares the components).
 __device__ __forceinline__ uint16_t code_of(const uint16_t* __restrict__ table, int Ng, int H,
                                             int qa, int qb, int qc) {
   if (qc < 0) {
@@ -90,21 +94,66 @@ __device__ __forceinline__ uint16_t code_of(const uint16_t* __restrict__ table, 
   return __ldg(table + ((int64_t)a * Ng + b) * H + qc);
 }
 
-__device__ __forceinline__ void add_run(uint32_t* H, int n, uint16_t c2, uint16_t c3,
-                                        uint32_t acc) {
-  if (!acc || (c2 & 0xFF) == 0xFF || (c3 & 0xFF) == 0xFF) return;
-  const int f2 = c2 & 0xFF, e2 = f2 + (c2 >> 8);
-  const int f3 = c3 & 0xFF, e3 = f3 + (c3 >> 8);
-  for (int y = f2; y <= e2; ++y)
-    for (int z = f3; z <= e3; ++z) atomicAdd(&H[y * n + z], acc);
+// Byte codes of the cube [-r, r]^3 (zero outside |q|^2 <= R2); flag[0] is set when a mode
+// lies in more than two shells (not representable: the caller falls back).
+__global__ void cube_codes_kernel(const uint16_t* __restrict__ table, int Ng, int r, int R2,
+                                  uint8_t* __restrict__ cube, int* __restrict__ flag) {
+  const int S = 2 * r + 1;
+  const int64_t total = (int64_t)S * S * S;
+  const int HN = Ng / 2 + 1;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int z = (int)(i % S) - r;
+    const int y = (int)((i / S) % S) - r;
+    const int x = (int)(i / ((int64_t)S * S)) - r;
+    uint8_t out = 0;
+    if (x * x + y * y + z * z <= R2) {
+      const uint16_t c = code_of(table, Ng, HN, x, y, z);
+      const int first = c & 0xFF, extra = c >> 8;
+      if (first != 0xFF) {
+        if (extra > 1 || first > 63) atomicOr(flag, 1);
+        out = (uint8_t)(0x80 | ((extra & 1) << 6) | (first & 63));
+      }
+    }
+    cube[i] = out;
+  }
+}
+
+__device__ __forceinline__ void add_run(uint32_t* H, int n, uint32_t c2, uint32_t c3,
+                                        uint32_t cnt) {
+  for (int y = code_first(c2); y <= code_last(c2); ++y)
+    for (int z = code_first(c3); z <= code_last(c3); ++z) atomicAdd(&H[y * n + z], cnt);
+}
+
+// One 32-point window of a line: lane l holds the codes of z = zb + l (valid for l < nv).
+// Lanes with equal (code2, code3) in a row form a segment; its first lane adds the
+// segment's count (2 per pair, 1 for the pair with |q3| = |q2|) with one atomic.
+__device__ __forceinline__ void count_window(uint32_t* H, int n, int lane, int zb, int nv,
+                                             uint32_t c2, uint32_t c3, int eq_mode, int z_eq) {
+  const bool valid = lane < nv;
+  const uint32_t key = (valid && (c2 & c3 & 0x80u)) ? ((c2 << 8) | c3) : 0u;
+  const uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, key, 1);
+  const bool start = valid && (lane == 0 || key != prev);
+  const uint32_t starts = __ballot_sync(0xFFFFFFFFu, start);
+  if (start && key) {
+    const uint32_t above = lane == 31 ? 0u : starts >> (lane + 1);
+    const int end = above ? lane + __ffs(above) : nv;
+    const int len = end - lane;
+    uint32_t cnt = 2u * (uint32_t)len;
+    if (eq_mode == 1) {
+      cnt = (uint32_t)len;
+    } else if (eq_mode == 2 && z_eq >= zb + lane && z_eq < zb + end) {
+      cnt -= 1u;
+    }
+    add_run(H, n, key >> 8, key & 0xFFu, cnt);
+  }
 }
 
 // Dynamic shared memory: G, Whi, Wlo (n (n + 1) / 2 uint64 each), then H (n * n uint32).
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
     enum_kernel(const Mode* __restrict__ modes, const Batch* __restrict__ batches, int n_batches,
-                int* __restrict__ next_batch, const uint16_t* __restrict__ table, int Ng,
-                int R2, int n, unsigned long long* __restrict__ g_cnt,
-                double* __restrict__ g_w) {
+                int* __restrict__ next_batch, const uint8_t* __restrict__ cube, int r, int R2,
+                int n, unsigned long long* __restrict__ g_cnt, double* __restrict__ g_w) {
   extern __shared__ unsigned long long smem_u64[];
   __shared__ int s_batch;
   const int np = n * (n + 1) / 2;
@@ -112,16 +161,8 @@ __global__ void __launch_bounds__(kThreads)
   unsigned long long* Whi = G + np;
   unsigned long long* Wlo = Whi + np;
   uint32_t* H = reinterpret_cast<uint32_t*>(Wlo + np);
-  const int HN = Ng / 2 + 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = isqrt_floor(R2);
-  const int side = 2 * r + 1;
-  const int lines = side * side;
-  auto row_base = [&](int qa, int qb) {  // table offset of (qa, qb, 0)
-    const int a = qa < 0 ? qa + Ng : qa;
-    const int b = qb < 0 ? qb + Ng : qb;
-    return ((int64_t)a * Ng + b) * HN;
-  };
+  const int S = 2 * r + 1;
   for (int i = threadIdx.x; i < n * n; i += kThreads) H[i] = 0u;
   while (true) {
     __syncthreads();  // the previous batch's flush has read G / W
@@ -135,51 +176,62 @@ __global__ void __launch_bounds__(kThreads)
       const Mode q1 = modes[m];
       const int x1 = q1.x, y1 = q1.y, z1 = q1.z;
       const int n1 = x1 * x1 + y1 * y1 + z1 * z1;
-      // one warp per z-line of q2 = (x2, y2, z), its lanes on 32 consecutive z: the table
-      // reads of q2 and q3 are contiguous, and lanes whose (q2, q3) memberships agree add
-      // their count with one shared-memory atomic (the lowest lane of each group)
-      for (int li = warp; li < lines; li += kWarps) {
-        const int x2 = li / side - r, y2 = li % side - r;
-        const int t1 = R2 - x2 * x2 - y2 * y2;
-        const int x3 = -(x1 + x2), y3 = -(y1 + y2);
-        const int t2 = R2 - x3 * x3 - y3 * y3;
-        if (t1 < 0 || t2 < 0) continue;  // warp-uniform
-        const int r1 = isqrt_floor(t1), r2 = isqrt_floor(t2);
-        // |q2|^2 <= R2: |z| <= r1;  |q3|^2 <= R2: |z1 + z| <= r2
-        const int lo = max(-r1, -z1 - r2);
-        int hi = min(r1, -z1 + r2);
-        // |q3|^2 <= |q2|^2  <=>  2 z1 z <= -(n1 + 2 (x1 x2 + y1 y2)) = D
-        const int D = -(n1 + 2 * (x1 * x2 + y1 * y2));
-        if (z1 == 0) {
-          if (D < 0) continue;
-        } else {
-          const int den = 2 * z1;  // z1 > 0: z <= floor(D / den)
-          hi = min(hi, D >= 0 ? D / den : -((-D + den - 1) / den));
-        }
-        // the one z with |q3| = |q2| (counted once, every other pair twice): 2 z1 z = D
-        const int z_eq = (z1 == 0) ? (D == 0 ? INT_MIN + 1 : INT_MIN)
-                                   : (D % (2 * z1) == 0 ? D / (2 * z1) : INT_MIN);
-        const int64_t b2p = row_base(x2, y2), b2n = row_base(-x2, -y2);
-        const int64_t b3p = row_base(x3, y3), b3n = row_base(-x3, -y3);
-        for (int z0 = lo; z0 <= hi; z0 += 32) {
-          const int z = z0 + lane;
-          uint32_t key = 0xFFFFFFFFu;
-          if (z <= hi) {
-            const int z3 = -(z1 + z);
-            const uint32_t c2 = __ldg(table + (z >= 0 ? b2p + z : b2n - z));
-            const uint32_t c3 = __ldg(table + (z3 >= 0 ? b3p + z3 : b3n - z3));
-            if ((c2 & 0xFF) != 0xFF && (c3 & 0xFF) != 0xFF) key = c2 | (c3 << 16);
-          }
-          const uint32_t group = __match_any_sync(0xFFFFFFFFu, key);
-          if (key != 0xFFFFFFFFu && lane == __ffs(group) - 1) {
-            // with z1 == 0 every pair of the half-lens has |q3| = |q2| when D == 0
-            uint32_t cnt = 2u * __popc(group);
+      // lines (x2, y2) with both |q2| <= r and |q1 + q2| <= r possible
+      const int xa = max(-r, -r - x1), xb = min(r, r - x1);
+      const int ya = max(-r, -r - y1), yb = min(r, r - y1);
+      const int ny = yb - ya + 1;
+      const int lines = (xb - xa + 1) * ny;
+      for (int l0 = warp * 32; l0 < lines; l0 += kWarps * 32) {
+        // each lane sets up one line of the block of 32: the z-interval of the half-lens
+        //   |q2|^2 <= R2: |z| <= r1;   |q3|^2 <= R2: |z1 + z| <= r2;
+        //   |q3|^2 <= |q2|^2  <=>  2 z1 z <= -(n1 + 2 (x1 x2 + y1 y2)) = D
+        int lo = 1, hi = 0, b2 = 0, b3 = 0, eq_mode = 0, z_eq = 0;
+        const int li = l0 + lane;
+        if (li < lines) {
+          const int x2 = xa + li / ny, y2 = ya + li % ny;
+          const int x3 = -(x1 + x2), y3 = -(y1 + y2);
+          const int t1 = R2 - x2 * x2 - y2 * y2;
+          const int t2 = R2 - x3 * x3 - y3 * y3;
+          if (t1 >= 0 && t2 >= 0) {
+            const int r1 = isqrt_floor(t1), r2 = isqrt_floor(t2);
+            lo = max(-r1, -z1 - r2);
+            hi = min(r1, -z1 + r2);
+            const int D = -(n1 + 2 * (x1 * x2 + y1 * y2));
             if (z1 == 0) {
-              if (z_eq == INT_MIN + 1) cnt = __popc(group);
-            } else if (z_eq >= z0 && z_eq < z0 + 32 && ((group >> (z_eq - z0)) & 1u)) {
-              cnt -= 1u;
+              if (D < 0) hi = lo - 1;
+              eq_mode = D == 0 ? 1 : 0;
+            } else {
+              const int den = 2 * z1;  // z1 > 0: z <= floor(D / den)
+              hi = min(hi, D >= 0 ? D / den : -((-D + den - 1) / den));
+              if (D % den == 0) {
+                eq_mode = 2;
+                z_eq = D / den;
+              }
             }
-            add_run(H, n, (uint16_t)(key & 0xFFFF), (uint16_t)(key >> 16), cnt);
+            b2 = ((x2 + r) * S + (y2 + r)) * S + r;        // cube index of (x2, y2, z) - z
+            b3 = ((x3 + r) * S + (y3 + r)) * S + r - z1;   // cube index of q3 + z
+          }
+        }
+        uint32_t todo = __ballot_sync(0xFFFFFFFFu, lo <= hi);
+        while (todo) {
+          const int k = __ffs(todo) - 1;
+          todo &= todo - 1;
+          const int klo = __shfl_sync(0xFFFFFFFFu, lo, k);
+          const int khi = __shfl_sync(0xFFFFFFFFu, hi, k);
+          const int kb2 = __shfl_sync(0xFFFFFFFFu, b2, k);
+          const int kb3 = __shfl_sync(0xFFFFFFFFu, b3, k);
+          const int kmode = __shfl_sync(0xFFFFFFFFu, eq_mode, k);
+          const int kzeq = __shfl_sync(0xFFFFFFFFu, z_eq, k);
+          for (int z0 = klo; z0 <= khi; z0 += 64) {
+            // both windows' loads before either window's counting
+            const int za = z0 + lane, zb = z0 + 32 + lane;
+            const uint32_t c2a = za <= khi ? __ldg(cube + kb2 + za) : 0u;
+            const uint32_t c3a = za <= khi ? __ldg(cube + kb3 - za) : 0u;
+            const uint32_t c2b = zb <= khi ? __ldg(cube + kb2 + zb) : 0u;
+            const uint32_t c3b = zb <= khi ? __ldg(cube + kb3 - zb) : 0u;
+            count_window(H, n, lane, z0, min(32, khi - z0 + 1), c2a, c3a, kmode, kzeq);
+            if (z0 + 32 <= khi)
+              count_window(H, n, lane, z0 + 32, min(32, khi - z0 - 31), c2b, c3b, kmode, kzeq);
           }
         }
       }
@@ -206,9 +258,8 @@ __global__ void __launch_bounds__(kThreads)
       __syncthreads();
     }
     // add the batch sums to every shell of the batch's membership run
-    const uint16_t code = modes[bt.begin].code;
-    const int f1 = code & 0xFF, e1 = f1 + (code >> 8);
-    for (int x = f1; x <= e1; ++x) {
+    const uint32_t code = modes[bt.begin].code;
+    for (int x = code_first(code); x <= code_last(code); ++x) {
       for (int p = threadIdx.x; p < np; p += kThreads) {
         if (G[p]) {
           const size_t o = (size_t)x * np + p;
@@ -224,21 +275,6 @@ __global__ void __launch_bounds__(kThreads)
 size_t enum_smem_bytes(int n) {
   return 3 * sizeof(unsigned long long) * (size_t)(n * (n + 1) / 2) +
          sizeof(uint32_t) * (size_t)n * n;
-}
-
-// One thread per octant point (x, y, z) in [0, r]^3: its membership code (0x00FF = none).
-__global__ void octant_codes_kernel(const uint16_t* __restrict__ table, int Ng, int r, int R2,
-                                    uint16_t* __restrict__ out) {
-  const int side = r + 1;
-  const int64_t total = (int64_t)side * side * side;
-  const int HN = Ng / 2 + 1;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int z = (int)(i % side);
-    const int y = (int)((i / side) % side);
-    const int x = (int)(i / ((int64_t)side * side));
-    out[i] = x * x + y * y + z * z <= R2 ? code_of(table, Ng, HN, x, y, z) : (uint16_t)0x00FF;
-  }
 }
 
 // Per triangle t = (a, b, c): N_tri = G[a][b, c]; k_mean of each role from the role sums.
@@ -274,35 +310,41 @@ bool gridinfo_enum_supported(const bsk_plan* p) {
 
 void gridinfo_enum(bsk_plan* p, const std::vector<HostTriangle>& tri, double* ntri,
                    double* kmean, cudaStream_t st) {
-  const int64_t T = (int64_t)tri.size();
   using namespace genum;
+  const int64_t T = (int64_t)tri.size();
   BSK_REQUIRE(gridinfo_enum_supported(p), BSK_ERR_STATE, "internal: enumeration unsupported");
   const int r = p->qmax;
   const int R2 = (r + 1) * (r + 1) - 1;  // every shell mode has |q| < qmax + 1
-  // octant modes of the plan's shells, sorted by membership run, then batched
-  const int side = r + 1;
-  const size_t n_oct = (size_t)side * side * side;
-  std::vector<uint16_t> codes(n_oct);
-  {
-    void* d = nullptr;
-    BSK_CHECK_CUDA(cudaMallocAsync(&d, n_oct * sizeof(uint16_t), st));
-    octant_codes_kernel<<<p->num_sms * 8, 256, 0, st>>>(p->table, p->Ng, r, R2, (uint16_t*)d);
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(codes.data(), d, n_oct * sizeof(uint16_t), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFreeAsync(d, st);
-    BSK_REQUIRE(e == cudaSuccess, BSK_ERR_CUDA,
-                std::string("grid information: octant codes: ") + cudaGetErrorString(e));
-  }
+  const int S = 2 * r + 1;
+  const size_t n_cube = (size_t)S * S * S;
+  // byte codes of the cube [-r, r]^3, kept on the device for the enumeration; the octant
+  // part is read back to list the q1 modes
+  char* cube_mem = nullptr;
+  BSK_CHECK_CUDA(cudaMallocAsync((void**)&cube_mem, n_cube + 256, st));
+  struct FreeCube {
+    char* w;
+    cudaStream_t s;
+    ~FreeCube() { cudaFreeAsync(w, s); }
+  } free_cube{cube_mem, st};
+  uint8_t* d_cube = (uint8_t*)cube_mem;
+  int* d_flag = (int*)(cube_mem + (n_cube + 15) / 16 * 16);
+  std::vector<uint8_t> cube(n_cube);
+  int flag = 0;
+  BSK_CHECK_CUDA(cudaMemsetAsync(d_flag, 0, sizeof(int), st));
+  cube_codes_kernel<<<p->num_sms * 8, 256, 0, st>>>(p->table, p->Ng, r, R2, d_cube, d_flag);
+  BSK_CHECK_CUDA(cudaGetLastError());
+  BSK_CHECK_CUDA(cudaMemcpyAsync(cube.data(), d_cube, n_cube, cudaMemcpyDeviceToHost, st));
+  BSK_CHECK_CUDA(cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BSK_CHECK_CUDA(cudaStreamSynchronize(st));
+  BSK_REQUIRE(flag == 0, BSK_ERR_STATE, "internal: a mode lies in more than two shells");
   std::vector<Mode> modes;
   for (int x = 0; x <= r; ++x)
     for (int y = 0; y <= r; ++y)
       for (int z = 0; z <= r; ++z) {
-        const uint16_t c = codes[((size_t)x * side + y) * side + z];
-        if ((c & 0xFF) != 0xFF) {
+        const uint8_t c = cube[((size_t)(x + r) * S + (y + r)) * S + (z + r)];
+        if (c & 0x80) {
           const double w = std::sqrt((double)(x * x + y * y + z * z)) * std::ldexp(1.0, kFrac);
-          modes.push_back(Mode{(int16_t)x, (int16_t)y, (int16_t)z, c,
+          modes.push_back(Mode{(int16_t)x, (int16_t)y, (int16_t)z, (uint16_t)c,
                                (unsigned long long)std::llround(w)});
         }
       }
@@ -357,7 +399,7 @@ void gridinfo_enum(bsk_plan* p, const std::vector<HostTriangle>& tri, double* nt
                                                                  smem));
     const int grid = std::max(1, std::min<int>((int)batches.size(), per_sm * p->num_sms));
     enum_kernel<<<grid, kThreads, smem, st>>>(d_modes, d_batches, (int)batches.size(), d_next,
-                                              p->table, p->Ng, R2, n, g_cnt, g_w);
+                                              d_cube, r, R2, n, g_cnt, g_w);
     BSK_CHECK_CUDA(cudaGetLastError());
   }
   const double kf = 2.0 * 3.14159265358979323846 / p->L;

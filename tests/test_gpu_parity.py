@@ -407,7 +407,7 @@ def test_schedule_covers_every_pair(cuda):
     tiles, sum_nc, rows = plan.triangles(tri).schedule()
     pairs = {(int(i), int(j)) for i, j, _ in tri}
     assert rows == len(pairs)
-    assert tiles >= -(-rows // 128) and sum_nc % 16 == 0
+    assert tiles >= -(-rows // 128) and sum_nc % 8 == 0
     assert len(tri) <= 128 * sum_nc
     plan.close()
 
