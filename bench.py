@@ -67,17 +67,24 @@ def parse():
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the per-bin error study against the FP64 GPU contraction")
-    ap.add_argument("--serve-requests", type=int, default=200,
+    ap.add_argument("--serve-requests", type=int, default=2000,
                     help="requests of the serving leg (0 = skip)")
-    ap.add_argument("--serve-rate", type=float, default=40.0, help="Poisson arrival rate, req/s")
-    ap.add_argument("--serve-full", action="store_true",
-                    help="serving mix with N=512 (10%%) as well; default mix is N in 64/128/256")
+    ap.add_argument("--serve-rate", type=float, default=SERVE_RATE,
+                    help="Poisson arrival rate, req/s")
+    ap.add_argument("--serve-small", action="store_true",
+                    help="serving mix without N=512 (weights renormalised)")
+    ap.add_argument("--serve-sweep", default="20,40,80,160,320",
+                    help="offered rates of the bf16x3 p99-vs-rate sweep ('' = none)")
+    ap.add_argument("--serve-sweep-requests", type=int, default=300)
     ap.add_argument("--serve-only", action="store_true", help="run only the serving leg")
     ap.add_argument("--precision-study", action="store_true",
                     help="run only the 512^3 cross-bispectrum precision study (equilateral, "
                          "isosceles m=2, squeezed bins; fp32/bf16/bf16x3 vs the FP64 contraction)")
     ap.add_argument("--precision-out", default=None,
                     help="with --precision-study: write the per-bin errors to this JSON file")
+    ap.add_argument("--no-studies", action="store_true",
+                    help="skip the 512^3 cross precision study and the 1024^3 resident / "
+                         "streamed runs that the headline line carries")
     ap.add_argument("--no-cold", action="store_true",
                     help="profiling runs only: skip the one-off FP64 grid information and "
                          "normalise by 1 (same kernels and timings in the step)")
@@ -388,15 +395,9 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        from oracle.cpu_baseline import ReferenceCPU
-        ref = ReferenceCPU(delta.cpu().numpy(), BOX, edges, tri)
-        try:
-            ref.step()  # warm-up (page faults, worker start)
-            est = ref.step()
-            cpu = {"value": 1.0 / est, "unit": "bispectra/s", "cores": ref.P, "kind": "port",
-                   "sample": ref.describe(), "sample_seconds": ref.last["sample_seconds"]}
-        finally:
-            ref.close()
+        cpu = cpu_sampled(delta.cpu().numpy(), edges, tri)
+        if args.workload == "mesh512_all":
+            cpu["full_256"] = cpu_full_256(value_256=None)
 
     line = {
         "metric": METRIC,
@@ -441,11 +442,21 @@ def run_ours(args):
     }
     if fp32:
         line["speedup_vs_fp32_plain"] = value / fp32["value"]
-    if args.serve_requests > 0 and world == 1:
+    studies = world == 1 and args.workload == "mesh512_all" and not args.no_studies
+    if studies or (args.serve_requests > 0 and world == 1):
         plan.close()
         del delta, host, bufs
         torch.cuda.empty_cache()
-        line["serving"] = run_serving(args, dev)
+    if studies:
+        line["precision_study"] = precision_study(args, dev)
+        line["mesh1024"] = mesh1024_study(args, dev)
+        torch.cuda.empty_cache()
+    if args.serve_requests > 0 and world == 1:
+        sweep = [float(v) for v in args.serve_sweep.split(",") if v.strip()]
+        line["serving"] = run_serving(args, dev, sweep=sweep)
+        line["serving"]["p99_bound_ms"] = SERVE_P99_BOUND_MS
+        line["serving"]["p99_within_bound"] = bool(
+            line["serving"].get("p99_ms", 1e30) <= SERVE_P99_BOUND_MS)
         if not args.no_fp32:
             torch.cuda.empty_cache()
             line["serving_fp32"] = run_serving(args, dev, precision="fp32")
@@ -455,24 +466,32 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def run_serving(args, dev, precision="bf16x3"):
+SERVE_SIZES = [64, 128, 256, 512]
+SERVE_WEIGHTS = [0.4, 0.3, 0.2, 0.1]
+SERVE_RATE = 40.0          # req/s of the stated operating point (cfg4 mix)
+SERVE_P99_BOUND_MS = 400.0  # stated p99 bound at that rate (bf16x3)
+
+
+def run_serving(args, dev, precision="bf16x3", sweep=()):
     """Continuous-batching leg: seeded Poisson stream of mixed bispectrum requests.
 
-    Mix: N in {64,128,256,512} with weights {.4,.3,.2,.1} (512 only with
-    --serve-full; otherwise the first three, renormalised), 30% cross <AAB>,
-    bin set uniform over {all triangles dk=2kf to kNyq/2, equilateral, squeezed
-    with k1 in [kf, 3kf] (index 0)}, L = 100 Mpc/h, lognormal meshes (a seeded
-    pool per N), bf16x3.  Every configuration is served once before the timed
-    stream (plans, graphs and grid information resident); latency = arrival to
-    result on the host.
+    Mix (the serving configuration): N in {64, 128, 256, 512} with weights
+    {.4, .3, .2, .1}, 30% cross <AAB>, bin set uniform over {all triangles dk=2kf
+    to kNyq/2, equilateral, squeezed with k1 in [kf, 3kf] (index 0)}, L = 100 Mpc/h,
+    lognormal meshes (a seeded pool per N), ``--serve-requests`` requests at
+    ``--serve-rate`` req/s.  ``--serve-small`` drops N = 512 (weights renormalised).
+    Before the stream, ``Scheduler.prepare`` admits the groups and captures every
+    (instance, bin set) graph and computes every grid information, so nothing of
+    that sits on the dispatch path; latency = arrival to result on the host.
+    ``sweep``: further offered rates, ``--serve-sweep-requests`` requests each, for
+    the p99-vs-rate curve.
     """
     import numpy as np
     import torch
 
     from bskit_gb300 import serving, synthetic
-    rng = np.random.default_rng(2024)
-    sizes = [64, 128, 256, 512] if args.serve_full else [64, 128, 256]
-    w = np.array([0.4, 0.3, 0.2, 0.1][:len(sizes)])
+    sizes = SERVE_SIZES[:3] if args.serve_small else SERVE_SIZES
+    w = np.array(SERVE_WEIGHTS[:len(sizes)])
     w = w / w.sum()
     box = 100.0
     kf = 2 * np.pi / box
@@ -484,56 +503,78 @@ def run_serving(args, dev, precision="bf16x3"):
     torch.cuda.synchronize()
     sets = ["all", "equilateral", "squeezed"]
 
-    def make(i, t):
-        n = int(rng.choice(sizes, p=w))
-        kind = sets[int(rng.integers(3))]
-        cross = rng.random() < 0.3
-        spec = dict(kmin=kf, kmax=n / 4 * kf, dk=2 * kf, triangle_type=kind,
+    def spec_of(n, kind):
+        return dict(kmin=kf, kmax=n / 4 * kf, dk=2 * kf, triangle_type=kind,
                     squeezed_bin_index=0)
-        p = pool[n]
-        second = p[(i + 1) % len(p)] if cross else None
-        return serving.Request(i, p[i % len(p)], box, spec, second=second, arrival=t,
-                               precision=precision)
+
+    def stream(rng, n_req, rate):
+        gaps = rng.exponential(1.0 / rate, size=n_req)
+        reqs = []
+        for i, t in enumerate(np.cumsum(gaps)):
+            n = int(rng.choice(sizes, p=w))
+            kind = sets[int(rng.integers(3))]
+            cross = rng.random() < 0.3
+            p = pool[n]
+            second = p[(i + 1) % len(p)] if cross else None
+            reqs.append(serving.Request(i, p[i % len(p)], box, spec_of(n, kind), second=second,
+                                        arrival=t, precision=precision))
+        return reqs
 
     server = serving.make_server(max_batch=4, device=dev)
-    warm = []
-    for n in sizes:
-        for kind in sets:
-            for cross in (False, True):
-                spec = dict(kmin=kf, kmax=n / 4 * kf, dk=2 * kf, triangle_type=kind,
-                            squeezed_bin_index=0)
-                warm.append(serving.Request(-1, pool[n][0], box, spec,
-                                            second=pool[n][1] if cross else None,
-                                            precision=precision))
+    warm = [serving.Request(-1, pool[n][0], box, spec_of(n, kind),
+                            second=pool[n][1] if cross else None, precision=precision)
+            for n in sizes for kind in sets for cross in (False, True)]
     t0 = time.perf_counter()
+    for n in sizes:  # ahead of the stream: groups, graphs and grid information
+        server.prepare([r for r in warm if r.nmesh == n], groups=1 if n >= 512 else 2)
     server.run(warm, realtime=False)
-    warm_s = time.perf_counter() - t0
-    server.done = []
-    gaps = rng.exponential(1.0 / args.serve_rate, size=args.serve_requests)
-    reqs = [make(i, t) for i, t in enumerate(np.cumsum(gaps))]
-    server.run(reqs, realtime=True)
-    stats = serving.latency_stats(reqs)
-    stats.update({"rate_rps": args.serve_rate, "mix": "N %s, weights %s, 30%% cross, "
-                  "all/equilateral/squeezed" % (sizes, [round(x, 3) for x in w]),
-                  "warmup_s": warm_s, "precision": precision, "max_batch": 4,
+    prep_s = time.perf_counter() - t0
+
+    def serve(reqs):
+        server.done = []
+        cap0 = server.backend.captures_at_dispatch
+        server.run(reqs, realtime=True)
+        st = serving.latency_stats(reqs)
+        st["graph_captures_at_dispatch"] = server.backend.captures_at_dispatch - cap0
+        return st
+
+    rng = np.random.default_rng(2024)
+    stats = serve(stream(rng, args.serve_requests, args.serve_rate))
+    stats.update({"rate_rps": args.serve_rate,
+                  "mix": "N %s, weights %s, 30%% cross, all/equilateral/squeezed"
+                         % (sizes, [round(x, 3) for x in w]),
+                  "prepare_s": prep_s, "precision": precision, "max_batch": 4,
+                  "batching": "per shell set (N, box, shell list), bin sets mixed",
                   "resident_groups": len(server.groups)})
+    if sweep:
+        curve = []
+        for rate in sweep:
+            st = serve(stream(np.random.default_rng(int(rate)), args.serve_sweep_requests, rate))
+            curve.append({"rate_rps": rate, "p50_ms": st.get("p50_ms"), "p99_ms": st.get("p99_ms"),
+                          "throughput_rps": st.get("throughput_rps")})
+            if st.get("throughput_rps", 0.0) < 0.8 * rate:
+                break  # saturated: served well below the offered rate
+        ok = [c["rate_rps"] for c in curve if c["p99_ms"] is not None
+              and c["p99_ms"] <= SERVE_P99_BOUND_MS and c["throughput_rps"] >= 0.9 * c["rate_rps"]]
+        stats["sweep"] = {"requests_per_rate": args.serve_sweep_requests, "curve": curve,
+                          "knee_rps": max(ok) if ok else None,
+                          "knee": "highest offered rate served at >= 90% of the rate with "
+                                  "p99 <= %.0f ms" % SERVE_P99_BOUND_MS}
     return stats
 
 
-def run_precision_study(args):
+def precision_study(args, dev):
     """512^3 cross bispectrum <d1 d1 d2>, d1 lognormal (L = 1000 Mpc/h, seed 1), d2 =
     1.5 d1 + white noise of variance 0.1 var(d1) (seed 2); bins of width 2 k_f from k_f
     to k_Nyq/2: equilateral, isosceles m = 2 (tolerance 0.1) and squeezed with k1 in
     [k_f, 3 k_f] (squeezed_bin_index 0).  Each precision is compared bin by bin with the
-    FP64 SIMT contraction of the same FP32 shell fields."""
+    FP64 SIMT contraction of the same FP32 shell fields; returns the record."""
     import numpy as np
     import torch
 
     from bskit_gb300 import bins, synthetic
     from bskit_gb300.engine import Plan
 
-    torch.cuda.set_device(0)
-    dev = torch.device("cuda", 0)
     n, box = 512, 1000.0
     kf = 2 * math.pi / box
     kw = dict(kmin=kf, kmax=128 * kf, dk=2 * kf)
@@ -575,6 +616,7 @@ def run_precision_study(args):
             well = b64[live].abs() >= 0.1 * babs[live]
             res[prec] = {"contraction_ms": ev[0].elapsed_time(ev[1]),
                          "max_rel": float(rel.max()), "median_rel": float(rel.median()),
+                         "n_bins_rel_gt_1e-5": int((rel > 1e-5).sum()),
                          "p99_rel": float(rel.quantile(0.99)),
                          "max_rel_well_conditioned": float(rel[well].max()) if bool(well.any())
                          else None,
@@ -589,7 +631,7 @@ def run_precision_study(args):
         with open(args.precision_out, "w") as f:
             json.dump({"triangles": {k: np.asarray(v).tolist() for k, v in sets.items()},
                        "per_bin": per_bin}, f)
-    print(json.dumps({
+    rec = {
         "metric": "precision study: per-bin error vs the FP64 contraction of the same fields",
         "config": {"workload": "512^3 cross bispectrum <d1 d1 d2>, L=1000 Mpc/h, d2 = 1.5 d1 + "
                                "noise (0.1 var d1), 63 shells dk=2kf to kNyq/2",
@@ -597,8 +639,127 @@ def run_precision_study(args):
         "reference": "FP64 SIMT contraction of the same FP32 shell fields",
         "normalised": "|B - B64| / (L^6/Ng^3 sum |I_i I_j I_l|)",
         "well_conditioned": "|B64| >= 0.1 * L^6/Ng^3 sum |I_i I_j I_l|",
-        "sets": out}))
+        "sets": out}
     plan.close()
+    del d1, d2, a1, a2
+    torch.cuda.empty_cache()
+    return rec
+
+
+def run_precision_study(args):
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps(precision_study(args, torch.device("cuda", 0))))
+
+
+def cpu_sampled(delta_host, edges, tri, steps=None):
+    """The reference algorithm on the host cores over its stratified sample: one sampled shell
+    per step until every sampled shell was transformed (or ``steps`` steps)."""
+    from oracle.cpu_baseline import ReferenceCPU
+    ref = ReferenceCPU(delta_host, BOX, edges, tri)
+    try:
+        t0 = time.perf_counter()
+        est = None
+        for _ in range(steps or len(ref.shells)):
+            est = ref.step()
+        return {"value": 1.0 / est, "unit": "bispectra/s", "cores": ref.P, "kind": "port",
+                "sample": ref.describe(), "sample_seconds": time.perf_counter() - t0,
+                "bins_timed": ref.n_tri, "seconds_per_bispectrum_extrapolated": est}
+    finally:
+        ref.close()
+
+
+def cpu_full_256(value_256=None):
+    """The reference algorithm in full (every shell, every bin, not extrapolated) on the 256^3
+    all-triangle workload (L = 500, 31 shells, 3321 bins, lognormal seed 1), beside the
+    sampled estimate of the same workload: the check of the sampled extrapolation."""
+    from bskit_gb300 import synthetic
+    from oracle.cpu_baseline import ReferenceCPU
+    edges, tri = workload_bins("mesh256_all")
+    d = synthetic.lognormal_mesh(256, 500.0, seed=1)
+    full = ReferenceCPU(d, 500.0, edges, tri, full=True)
+    try:
+        secs, _ = full.full_run()
+        P = full.P
+    finally:
+        full.close()
+    samp = ReferenceCPU(d, 500.0, edges, tri, sample_shells=12)
+    try:
+        est = None
+        for _ in range(len(samp.shells)):
+            est = samp.step()
+    finally:
+        samp.close()
+    rec = {"workload": WORKLOADS["mesh256_all"][4], "cores": P, "measured_s": secs,
+           "bispectra_per_s": 1.0 / secs, "sampled_estimate_s": est,
+           "sampled_over_measured": est / secs,
+           "note": "full run: every shell c2r and all 3321 triangle sums, not extrapolated"}
+    if value_256:
+        rec["gpu_bispectra_per_s"] = value_256
+    return rec
+
+
+def mesh1024_study(args, dev, steps=5):
+    """1024^3 all-triangle auto bispectrum (L = 2000 Mpc/h, 38 shells of width 4 k_f to
+    0.3 k_Nyq, 5833 bins), bf16x3, normalised by the grid information: resident (reduced
+    480^3 grid, every shell field in HBM) and streamed in chunks of 16 shells (a plan budget
+    with room for 16-shell buffers only).  Bispectra/s of each, the grid-information time,
+    and the largest difference between the two results over the largest |B|."""
+    import torch
+
+    from bskit_gb300 import synthetic
+    from bskit_gb300.engine import Plan
+    edges, tri = workload_bins("mesh1024_all")
+    n, box = 1024, 2000.0
+    delta = synthetic.lognormal_mesh_torch(n, box, seed=1, device=dev).contiguous()
+    stream = torch.cuda.current_stream()
+
+    def run(plan, ts, ntri):
+        def step():
+            plan.paint(0, delta)
+            return plan.normalize(plan.measure_b(ts, precision="bf16x3"), ntri)
+        step()
+        plan.sync_check()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            b = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plan.sync_check()
+        ms = e0.elapsed_time(e1) / steps
+        return {"ms_per_step": ms, "bispectra_per_s": 1e3 / ms}, b
+
+    plan = Plan(n, box, edges, device=dev)
+    ts = plan.triangles(tri)
+    t0 = time.perf_counter()
+    ntri, _ = plan.gridinfo(ts)
+    plan.sync_check()
+    gi_s = time.perf_counter() - t0
+    resident, b_res = run(plan, ts, ntri)
+    resident["footprint_gb"] = plan.footprint() / 1e9
+    ng = plan.ngrid
+    plan.close()
+    torch.cuda.empty_cache()
+    probe = Plan(n, box, edges, device=dev)
+    probe.paint(0, delta)
+    fp0 = probe.footprint()
+    probe.close()
+    K = ng ** 3
+    sp = Plan(n, box, edges, mem_budget=fp0 + 20 * 16 * K, device=dev)
+    ts2 = sp.triangles(tri)
+    streamed, b_str = run(sp, ts2, ntri)
+    streamed["chunk_shells"] = sp.stream_chunk()
+    streamed["budget_gb"] = (fp0 + 20 * 16 * K) / 1e9
+    sp.close()
+    ok = ntri > 0
+    diff = float(((b_str - b_res).abs()[ok]).max() / b_res[ok].abs().max())
+    del delta
+    torch.cuda.empty_cache()
+    return {"workload": WORKLOADS["mesh1024_all"][4], "contraction_grid": ng,
+            "precision": "bf16x3", "gridinfo_s": gi_s, "resident": resident,
+            "streamed": streamed, "max_abs_diff_over_max_abs_B": diff, "steps": steps}
 
 
 def run_reference(args):
@@ -617,9 +778,9 @@ def run_reference(args):
         for _ in range(args.warmup):
             ref.step()
         t0 = time.perf_counter()
-        ests = [ref.step() for _ in range(args.steps)]
+        for _ in range(args.steps):
+            est = ref.step()  # cumulative: every bin and shell timed so far
         wall = time.perf_counter() - t0
-        est = float(np.mean(ests))
         value = 1.0 / est
         line = {
             "impl": "reference", "metric": METRIC, "value": value, "unit": "bispectra/s",
@@ -633,10 +794,13 @@ def run_reference(args):
             "e2e": {"value": value, "unit": "bispectra/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "sample_wall_s": wall,
+            "bins_timed": ref.n_tri,
         }
-        print(json.dumps(line))
     finally:
         ref.close()
+    if args.workload == "mesh512_all":
+        line["full_256"] = cpu_full_256()
+    print(json.dumps(line))
 
 
 def main():

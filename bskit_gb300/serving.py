@@ -11,12 +11,20 @@ types) and a precision.  The server
 * admits work by HBM footprint: a group of engine instances for a shell set is
   created only when its measured footprint fits in the budget (idle groups of
   other shell sets are evicted, least recently used first);
-* batches requests that share a bin set into one captured CUDA graph per batch
-  size (paint -> shell fields -> contraction -> normalisation -> device-to-host
-  copy of B for every request of the batch, as parallel graph branches);
-* runs batches of different groups on different CUDA streams, so requests
-  that arrive while others are on the GPU start as soon as a group and memory
-  are free and their work overlaps on the device;
+* batches requests of one shell set -- one N_grid, box and shell list -- whatever
+  their bin sets (all / equilateral / squeezed / isosceles, auto or cross) and
+  precisions: a batch of up to ``max_batch`` such requests runs on the instances
+  of one group, request k on instance k;
+* runs every request as a CUDA graph (paint -> shell fields -> contraction ->
+  normalisation -> device-to-host copy of B) captured once per (instance, bin
+  set): ``Scheduler.prepare`` captures them ahead of the stream for the
+  configurations it is given, so no capture sits on the dispatch path of a
+  prepared configuration (a configuration first seen in the stream is captured
+  when first dispatched);
+* replays the graphs of a batch on the group's per-instance streams, and batches
+  of different groups on theirs, so requests that arrive while others are on the
+  GPU start as soon as an instance and memory are free and their work overlaps on
+  the device;
 * records arrival, dispatch and completion times (p50 / p99 latency).
 
 The scheduling logic (``Scheduler``) is independent of CUDA; ``EngineBackend``
@@ -101,7 +109,7 @@ def bin_lists(spec, num_fields=1):
 
 
 class Job(object):
-    """Scheduler view of a request: its shell-set key and bin-set key."""
+    """Scheduler view of a request: its shell-set key (the batching key) and bin-set key."""
 
     def __init__(self, req):
         self.req = req
@@ -127,7 +135,7 @@ class Scheduler(object):
         self.max_batch = int(max_batch)
         self.max_groups = int(max_groups)   # per shell set
         self.clock = clock
-        self.pending = collections.OrderedDict()   # bin_key -> deque of jobs (FIFO)
+        self.pending = collections.OrderedDict()   # shell_key -> deque of jobs (FIFO)
         self.groups = []                           # all resident groups
         self.busy = {}                             # group -> (batch, jobs)
         self.last_used = {}
@@ -138,8 +146,27 @@ class Scheduler(object):
     # -------------------------------------------------------------- intake
     def submit(self, req):
         job = Job(req)
-        self.pending.setdefault(job.bin_key, collections.deque()).append(job)
+        self.pending.setdefault(job.shell_key, collections.deque()).append(job)
         return job
+
+    def prepare(self, requests, groups=None):
+        """Admit up to ``groups`` (default max_groups) groups per shell set of the given
+        configurations and capture, on every instance, the graph of every bin set among
+        them, before any request is served."""
+        jobs = [Job(r) for r in requests]
+        per_shell = collections.OrderedDict()
+        for j in jobs:
+            per_shell.setdefault(j.shell_key, []).append(j)
+        want = self.max_groups if groups is None else int(groups)
+        for key, js in per_shell.items():
+            while sum(1 for g in self.groups if g.shell_key == key) < want:
+                if self._admit_group(js[0]) is None:
+                    break
+            for g in self.groups:
+                if g.shell_key == key:
+                    for j in js:
+                        self.backend.prepare(g, j)
+        return jobs
 
     def n_pending(self):
         return sum(len(q) for q in self.pending.values())
@@ -194,7 +221,8 @@ class Scheduler(object):
                     self.done.append(j.req)
                 del self.busy[g]
                 self.last_used[g] = t
-        # oldest waiting request first
+        # the shell set whose oldest request waits longest first; a batch takes that set's
+        # requests in arrival order, whatever their bin sets
         order = sorted(self.pending.keys(), key=lambda k: self.pending[k][0].req.arrival
                        if self.pending[k] else float("inf"))
         for key in order:
@@ -209,6 +237,7 @@ class Scheduler(object):
                 t = self.clock()
                 for j in jobs:
                     j.req.t_dispatch = t
+                self.log.append(("batch", key[:2], len(jobs), len({j.bin_key for j in jobs})))
                 self.busy[g] = (self.backend.launch(g, jobs), jobs)
                 self.last_used[g] = t
             if not q:
@@ -255,7 +284,7 @@ class _Group(object):
 
 
 class EngineBackend(object):
-    """Drives the CUDA engine: one plan per instance, graphs per (bin set, batch size)."""
+    """Drives the CUDA engine: one plan per instance, one graph per (instance, bin set)."""
 
     def __init__(self, device=None, use_graphs=True):
         import torch
@@ -265,6 +294,8 @@ class EngineBackend(object):
         self.use_graphs = use_graphs
         self.gridinfo = {}      # bin_key -> (ntri, kmean) device tensors
         self.probe = {}         # shell_key -> measured footprint of one instance
+        self.captures = 0       # graphs captured (prepare + dispatch)
+        self.captures_at_dispatch = 0
 
     # -------------------------------------------------------------- resources
     def _new_instance(self, job):
@@ -278,10 +309,14 @@ class EngineBackend(object):
                       for _ in range(2)]
         inst.tsets = {}
         inst.out = {}
+        inst.graphs = {}
+        inst.warm = set()
         return inst
 
     def _warm(self, inst, job):
         """One eager run so that every lazily allocated buffer exists before capture."""
+        if job.bin_key in inst.warm:
+            return
         torch = self.torch
         slots = (0, 0, 1) if job.req.num_fields == 2 else (0, 0, 0)
         for s in range(job.req.num_fields):
@@ -290,6 +325,7 @@ class EngineBackend(object):
         ts = self._tset(inst, job)
         inst.plan.measure_b(ts, slots=slots, precision=job.req.precision)
         torch.cuda.synchronize(self.device)
+        inst.warm.add(job.bin_key)
 
     def _tset(self, inst, job):
         ts = inst.tsets.get(job.bin_key)
@@ -299,12 +335,19 @@ class EngineBackend(object):
         return ts
 
     def group_footprint(self, job, size):
-        fp = self.probe.get((job.shell_key, job.req.num_fields))
+        fp = self.probe.get(job.shell_key)
         if fp is None:
+            # an instance serves auto and cross requests of its shell set alike: measure it
+            # with both field slots built
             inst = self._new_instance(job)
             self._warm(inst, job)
+            inst.dmesh[1].zero_()
+            inst.plan.paint(1, inst.dmesh[1])
+            inst.plan.measure_b(self._tset(inst, job), slots=(0, 0, 1),
+                                precision=job.req.precision)
+            self.torch.cuda.synchronize(self.device)
             fp = inst.plan.footprint() + 2 * job.req.nmesh ** 3 * 4
-            self.probe[(job.shell_key, job.req.num_fields)] = fp
+            self.probe[job.shell_key] = fp
             inst.plan.close()
         return fp * size
 
@@ -313,14 +356,12 @@ class EngineBackend(object):
         g = _Group(job.shell_key, size)
         g.instances = [self._new_instance(job) for _ in range(size)]
         g.streams = [torch.cuda.Stream(device=self.device) for _ in range(size)]
-        g.graphs = {}
         return g
 
     def destroy_group(self, g):
         for inst in g.instances:
             inst.plan.close()
         g.instances = []
-        g.graphs = {}
 
     # -------------------------------------------------------------- grid info
     def _gridinfo(self, inst, job):
@@ -353,76 +394,69 @@ class EngineBackend(object):
         out[1].copy_(b, non_blocking=True)
         return out
 
-    def _graph(self, g, jobs):
-        """Captured graph running len(jobs) pipelines of one bin set as parallel branches."""
+    def _graph(self, inst, stream, job):
+        """The instance's captured pipeline for the job's bin set (captured on first use)."""
         torch = self.torch
-        key = (jobs[0].bin_key, len(jobs))
-        gr = g.graphs.get(key)
-        if gr is not None:
-            return gr
-        for inst in g.instances[:len(jobs)]:
-            self._warm(inst, jobs[0])
-        ntri = self._gridinfo(g.instances[0], jobs[0])[0]
-        for inst in g.instances[:len(jobs)]:
-            self._enqueue(inst, jobs[0], ntri)  # allocate pinned outputs eagerly
+        graph = inst.graphs.get(job.bin_key)
+        if graph is not None:
+            return graph
+        self._warm(inst, job)
+        ntri = self._gridinfo(inst, job)[0]
+        self._enqueue(inst, job, ntri)  # allocate the pinned outputs eagerly
         torch.cuda.synchronize(self.device)
         graph = torch.cuda.CUDAGraph()
-        cap = torch.cuda.Stream(device=self.device)
-        with torch.cuda.graph(graph, stream=cap, capture_error_mode="thread_local"):
-            fork = torch.cuda.current_stream()
-            start = torch.cuda.Event()
-            start.record(fork)
-            ends = []
-            for k, inst in enumerate(g.instances[:len(jobs)]):
-                s = g.streams[k]
-                s.wait_event(start)
-                with torch.cuda.stream(s):
-                    self._enqueue(inst, jobs[0], ntri)
-                    e = torch.cuda.Event()
-                    e.record(s)
-                    ends.append(e)
-            for e in ends:
-                fork.wait_event(e)
-        g.graphs[key] = graph
+        with torch.cuda.graph(graph, stream=stream, capture_error_mode="thread_local"):
+            self._enqueue(inst, job, ntri)
+        inst.graphs[job.bin_key] = graph
+        self.captures += 1
         return graph
+
+    def prepare(self, g, job):
+        """Capture the job's bin-set graph on every instance of the group (ahead of serving)."""
+        if not self.use_graphs:
+            for inst in g.instances:
+                self._warm(inst, job)
+                self._gridinfo(inst, job)
+            return
+        for inst, stream in zip(g.instances, g.streams):
+            self._graph(inst, stream, job)
 
     def launch(self, g, jobs):
         torch = self.torch
-        stream = g.streams[0]
-        ntri, kmean = self._gridinfo(g.instances[0], jobs[0])
-        # capture (first batch of this bin set and size only) before the meshes are staged:
-        # the warm-up run of the capture overwrites the instances' mesh buffers
-        graph = self._graph(g, jobs) if self.use_graphs else None
-        # host -> device copies of the batch's meshes (from the requests' own buffers)
-        with torch.cuda.stream(stream):
-            for inst, job in zip(g.instances, jobs):
+        done = []
+        for k, job in enumerate(jobs):
+            inst, stream = g.instances[k], g.streams[k]
+            ntri, kmean = self._gridinfo(inst, job)
+            graph = None
+            if self.use_graphs:
+                if job.bin_key not in inst.graphs:
+                    self.captures_at_dispatch += 1
+                # capture before this request's mesh is staged: the capture's warm-up run
+                # overwrites the instance's mesh buffers
+                graph = self._graph(inst, stream, job)
+            with torch.cuda.stream(stream):
                 inst.dmesh[0].copy_(torch.as_tensor(job.req.mesh), non_blocking=True)
                 if job.req.num_fields == 2:
                     inst.dmesh[1].copy_(torch.as_tensor(job.req.second), non_blocking=True)
-        if graph is not None:
-            with torch.cuda.stream(stream):
-                graph.replay()
-        else:
-            with torch.cuda.stream(stream):
-                for inst, job in zip(g.instances, jobs):
+                if graph is not None:
+                    graph.replay()
+                else:
                     self._enqueue(inst, job, ntri)
-        done = torch.cuda.Event()
-        done.record(stream)
-        return (done, g, jobs, kmean, ntri)
+                e = torch.cuda.Event()
+                e.record(stream)
+            done.append((e, inst, job, ntri, kmean))
+        return done
 
     def poll(self, batch):
-        done, g, jobs, kmean, ntri = batch
-        if not done.query():
+        if not all(e.query() for e, _, _, _, _ in batch):
             return False
-        u = jobs[0].req.spec.get("pos_units_mpcoverh", 1.0)
-        nt = ntri.cpu().numpy()
-        km = kmean.cpu().numpy()
-        for inst, job in zip(g.instances, jobs):
+        for _, inst, job, ntri, kmean in batch:
+            u = job.req.spec.get("pos_units_mpcoverh", 1.0)
             out = inst.out[job.bin_key]
             job.req.B = out[0].numpy().copy() * u ** 6
             job.req.B_unnorm = out[1].numpy().copy() * u ** 6
-            job.req.N_tri = nt
-            job.req.k_mean = km / u
+            job.req.N_tri = ntri.cpu().numpy()
+            job.req.k_mean = kmean.cpu().numpy() / u
         return True
 
 

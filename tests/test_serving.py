@@ -26,6 +26,8 @@ class FakeBackend(object):
         self.created = []
         self.destroyed = []
         self.launched = []
+        self.order = []
+        self.prepared = []
 
     def group_footprint(self, job, size):
         return 10 * job.req.nmesh * size
@@ -40,7 +42,11 @@ class FakeBackend(object):
 
     def launch(self, g, jobs):
         self.launched.append((g.shell_key[0], len(jobs)))
+        self.order.extend(j.req.rid for j in jobs)
         return {"left": 5, "jobs": jobs}
+
+    def prepare(self, g, job):
+        self.prepared.append((g.shell_key[0], job.req.spec["triangle_type"]))
 
     def poll(self, batch):
         batch["left"] -= 1
@@ -58,19 +64,38 @@ def _req(rid, n, t="all", arrival=0.0, cross=False):
     return serving.Request(rid, mesh, 100.0, spec, second=mesh if cross else None, arrival=arrival)
 
 
-def test_batches_share_bin_sets_and_fifo():
+def test_batches_mix_bin_sets_of_one_shell_set_in_arrival_order():
     be = FakeBackend()
     sch = serving.Scheduler(be, mem_budget=10 ** 6, max_batch=4, max_groups=3, clock=FakeClock())
-    reqs = [_req(i, 16, "all" if i % 2 == 0 else "equilateral") for i in range(10)]
+    reqs = [_req(i, 32, "all" if i % 2 == 0 else "equilateral", arrival=1e-3 * i)
+            for i in range(10)]
     sch.run(reqs, realtime=False)
     assert all(r.B is not None and r.B[0] == r.rid for r in reqs)
-    # every batch holds one bin set and at most max_batch requests
+    # one shell set (both bin sets share the shells): batches of up to max_batch requests
+    # that mix the bin sets, dispatched in arrival order
     assert all(1 <= k <= 4 for _, k in be.launched)
     assert sum(k for _, k in be.launched) == 10
-    # groups are per shell set (both bin sets share the shells); busy groups scale out
-    assert all(c == (16, 4) for c in be.created) and 1 <= len(be.created) <= 3
+    assert be.order == list(range(10))
+    mixed = [e for e in sch.log if e[0] == "batch" and e[3] > 1]
+    assert mixed, "no batch held two bin sets"
+    # groups are per shell set; busy groups scale out
+    assert all(c == (32, 4) for c in be.created) and 1 <= len(be.created) <= 3
     lat = serving.latency_stats(reqs)
     assert lat["requests"] == 10 and lat["p99_ms"] >= lat["p50_ms"]
+
+
+def test_prepare_admits_groups_and_captures_every_bin_set_ahead():
+    be = FakeBackend()
+    sch = serving.Scheduler(be, mem_budget=10 ** 6, max_batch=2, max_groups=2, clock=FakeClock())
+    cfg = [_req(0, 16, "all"), _req(1, 16, "equilateral"), _req(2, 32, "squeezed")]
+    sch.prepare(cfg)
+    # two groups per shell set, every bin set of the set captured on each
+    assert sorted(be.created) == [(16, 2), (16, 2), (32, 2), (32, 2)]
+    assert sorted(be.prepared) == sorted([(16, "all"), (16, "equilateral")] * 2 +
+                                         [(32, "squeezed")] * 2)
+    reqs = [_req(i, 16, "all" if i % 2 else "equilateral") for i in range(6)]
+    sch.run(reqs, realtime=False)
+    assert len(be.created) == 4 and all(r.B is not None for r in reqs)
 
 
 def test_admission_by_footprint_and_eviction():
@@ -151,6 +176,8 @@ def test_mixed_stream_equals_each_request_alone(cuda):
     mixed = serving.make_server(mem_budget=40 << 30, max_batch=3)
     mixed.run([serving.Request(r.rid, r.mesh, r.box, r.spec, r.second) for r in reqs],
               realtime=False)
+    # batches of one N mix bin sets (all / equilateral / squeezed, auto and cross)
+    assert any(e[0] == "batch" and e[3] > 1 for e in mixed.log)
     got = {r.rid: r for r in mixed.done}
     for r in reqs:
         alone = serving.make_server(mem_budget=40 << 30, max_batch=1, use_graphs=False)
