@@ -1,5 +1,6 @@
 // SIMT triple-product contraction: the plain-FP32 path and the FP64 GPU oracle.
 //
+// The FP64 variants (FP32 or FP64 fields, FP64 products and sums):
 // Work item = (sub-tile of 128 pair rows x 32 third-shell columns, K slice).
 // Per 32-point chunk the block forms the 128 pair products P[r][x] =
 // F1[i_r](x) * F2[j_r](x) and the 32 column values F3[l](x) in shared memory
@@ -138,6 +139,122 @@ __global__ void __launch_bounds__(THREADS) contract_simt_kernel(
   }
 }
 
+// ---------------------------------------------------------------- plain FP32 path
+// Work item = (tile of 128 pair rows x up to 64 column shells, 8192-point slice).  Per
+// 32-point chunk the block copies the tile's source rows (coalesced) and its column rows
+// into shared memory, forms the 128 x 32 pair products P = F1_i F2_j there, and each warp
+// runs a 32-row x 32-column block of the outer product, 8 rows x 4 columns per thread
+// (two 16-byte loads of P and one of F3 per 32 FMAs).  Warps whose 32 columns lie past the
+// tile's nc skip their multiply-adds.  FP32 sums over the slice, FP64 atomics across slices.
+namespace f32 {
+constexpr int KC = 32;
+constexpr int THREADS = 256;
+constexpr int ROWS = 128, COLS = 64, SRC = 64;
+constexpr int APITCH = ROWS + 4;    // A[x][r]
+constexpr int BPITCH = COLS + 4;    // B[x][c]
+constexpr int SPITCH = KC + 1;      // S[row][x]
+constexpr int64_t SLICE = 8192;
+
+struct Smem {
+  float A[KC][APITCH];
+  float B[KC][BPITCH];
+  float S1[SRC][SPITCH];
+  float S2[SRC][SPITCH];
+};
+
+__global__ void __launch_bounds__(THREADS, 2)
+    contract_f32_kernel(const TileDesc* __restrict__ tiles, int n_tiles,
+                        const int16_t* __restrict__ row_i, const int16_t* __restrict__ row_j,
+                        const int32_t* __restrict__ map, const float* __restrict__ f1,
+                        const float* __restrict__ f2, const float* __restrict__ f3,
+                        int n_shells, int64_t K, int64_t k_begin, int64_t k_end,
+                        int64_t n_slices, double* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char f32_smem[];
+  Smem& sm = *reinterpret_cast<Smem*>(f32_smem);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // outer-product block of this warp: rows [32 wr, +32), columns [32 wc, +32)
+  const int wr = warp & 3, wc = warp >> 2;
+  const int r0 = 32 * wr + 8 * (lane >> 3);   // this thread's 8 rows
+  const int c0 = 32 * wc + 4 * (lane & 7);    // and 4 columns
+  // pair-product formation: row fr, points [16 fh, +16)
+  const int fr = tid & (ROWS - 1), fh = tid >> 7;
+  const int64_t n_items = (int64_t)n_tiles * n_slices;
+  for (int64_t item = blockIdx.x; item < n_items; item += gridDim.x) {
+    const int64_t sl = item / n_tiles;
+    const TileDesc td = tiles[item % n_tiles];
+    const bool one_src = f1 == f2 && td.i0 == td.j0;
+    const int ri = row_i[td.row_off + fr], rj = row_j[td.row_off + fr];
+    const int pi = ri >= 0 ? ri - td.i0 : -1, pj = ri >= 0 ? rj - td.j0 : -1;
+    const bool busy = 32 * wc < td.nc;
+    const int64_t x_begin = k_begin + sl * SLICE;
+    const int64_t x_end = min(k_end, x_begin + SLICE);
+    float acc[8][4];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
+    for (int64_t x0 = x_begin; x0 < x_end; x0 += KC) {
+      const int x = (int)(tid & 31);
+      const bool xin = x0 + x < x_end;
+      // source rows and column rows of the chunk (lanes along points: coalesced)
+      for (int row = tid >> 5; row < SRC; row += THREADS / 32) {
+        const int s1 = td.i0 + row;
+        sm.S1[row][x] = (row < td.ni && s1 < n_shells && xin) ? __ldg(f1 + (int64_t)s1 * K + x0 + x)
+                                                               : 0.f;
+        if (!one_src) {
+          const int s2 = td.j0 + row;
+          sm.S2[row][x] = (row < td.nj && s2 < n_shells && xin)
+                              ? __ldg(f2 + (int64_t)s2 * K + x0 + x) : 0.f;
+        }
+      }
+      for (int c = tid >> 5; c < COLS; c += THREADS / 32) {
+        const int l = td.l0 + c;
+        sm.B[x][c] = (c < td.nc && l < n_shells && xin) ? __ldg(f3 + (int64_t)l * K + x0 + x)
+                                                        : 0.f;
+      }
+      __syncthreads();
+      {
+        const float(*S2)[SPITCH] = one_src ? sm.S1 : sm.S2;
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          const int xx = 16 * fh + e;
+          sm.A[xx][fr] = pi >= 0 ? sm.S1[pi][xx] * S2[pj][xx] : 0.f;
+        }
+      }
+      __syncthreads();
+      if (busy) {
+#pragma unroll 8
+        for (int k = 0; k < KC; ++k) {
+          const float4 a0 = *reinterpret_cast<const float4*>(&sm.A[k][r0]);
+          const float4 a1 = *reinterpret_cast<const float4*>(&sm.A[k][r0 + 4]);
+          const float4 b = *reinterpret_cast<const float4*>(&sm.B[k][c0]);
+          const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+          const float bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+          for (int p = 0; p < 8; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(av[p], bv[q], acc[p][q]);
+        }
+      }
+      __syncthreads();
+    }
+    if (busy) {
+#pragma unroll
+      for (int p = 0; p < 8; ++p) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int c = c0 + q;
+          if (c < td.nc) {
+            const int t = __ldg(map + td.map_off + c * kTileRows + r0 + p);
+            if (t >= 0) atomicAdd(out + t, (double)acc[p][q]);
+          }
+        }
+      }
+    }
+  }
+}
+}  // namespace f32
+
 template <typename Tin, typename Tacc>
 void launch_simt(const DeviceSchedule& s, const Tin* f1, const Tin* f2, const Tin* f3,
                  int n_shells, int64_t K, int64_t k_begin, int64_t k_end, int64_t slice,
@@ -162,11 +279,26 @@ void launch_simt(const DeviceSchedule& s, const Tin* f1, const Tin* f2, const Ti
 
 }  // namespace
 
-// FP32 products and tile sums, 4096-point slices, FP64 cross-slice sum.
+// FP32 products and tile sums (8192-point slices), FP64 cross-slice sum.
 void launch_contract_simt_f32(const DeviceSchedule& s, const float* f1, const float* f2,
                               const float* f3, int n_shells, int64_t K, int64_t k_begin,
                               int64_t k_end, double* out, int num_sms, cudaStream_t st) {
-  launch_simt<float, float>(s, f1, f2, f3, n_shells, K, k_begin, k_end, 4096, out, num_sms, st);
+  if (s.n_tiles == 0 || k_end <= k_begin) return;
+  const size_t smem = sizeof(f32::Smem);
+  BSK_CHECK_CUDA(cudaFuncSetAttribute(f32::contract_f32_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  BSK_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, f32::contract_f32_kernel, f32::THREADS, smem));
+  if (per_sm < 1) per_sm = 1;
+  const int64_t n_slices = (k_end - k_begin + f32::SLICE - 1) / f32::SLICE;
+  const int64_t n_items = n_slices * s.n_tiles;
+  int64_t grid = (int64_t)num_sms * per_sm;
+  if (grid > n_items) grid = n_items;
+  f32::contract_f32_kernel<<<(unsigned)grid, f32::THREADS, smem, st>>>(
+      s.tiles, s.n_tiles, s.row_i, s.row_j, s.map, f1, f2, f3, n_shells, K, k_begin, k_end,
+      n_slices, out);
+  BSK_CHECK_CUDA(cudaGetLastError());
 }
 
 // FP64 products and sums of FP32 fields (the GPU oracle of the precision study).

@@ -48,6 +48,7 @@ namespace genum {
 
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
+constexpr int kWin = 4;                            // 32-point windows whose loads overlap
 constexpr int kMaxShells = 64;                     // tables of at most 64 shells
 constexpr int kMaxBatch = 32;                      // octant modes per batch
 constexpr int kFrac = 44;                          // fractional bits of the |q| weights
@@ -222,16 +223,21 @@ __global__ void __launch_bounds__(kThreads, 2)
           const int kb3 = __shfl_sync(0xFFFFFFFFu, b3, k);
           const int kmode = __shfl_sync(0xFFFFFFFFu, eq_mode, k);
           const int kzeq = __shfl_sync(0xFFFFFFFFu, z_eq, k);
-          for (int z0 = klo; z0 <= khi; z0 += 64) {
-            // both windows' loads before either window's counting
-            const int za = z0 + lane, zb = z0 + 32 + lane;
-            const uint32_t c2a = za <= khi ? __ldg(cube + kb2 + za) : 0u;
-            const uint32_t c3a = za <= khi ? __ldg(cube + kb3 - za) : 0u;
-            const uint32_t c2b = zb <= khi ? __ldg(cube + kb2 + zb) : 0u;
-            const uint32_t c3b = zb <= khi ? __ldg(cube + kb3 - zb) : 0u;
-            count_window(H, n, lane, z0, min(32, khi - z0 + 1), c2a, c3a, kmode, kzeq);
-            if (z0 + 32 <= khi)
-              count_window(H, n, lane, z0 + 32, min(32, khi - z0 - 31), c2b, c3b, kmode, kzeq);
+          for (int z0 = klo; z0 <= khi; z0 += 32 * kWin) {
+            // every window's loads before any window's counting: kWin L2 round trips overlap
+            uint32_t c2[kWin], c3[kWin];
+#pragma unroll
+            for (int u = 0; u < kWin; ++u) {
+              const int z = z0 + 32 * u + lane;
+              c2[u] = z <= khi ? __ldg(cube + kb2 + z) : 0u;
+              c3[u] = z <= khi ? __ldg(cube + kb3 - z) : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < kWin; ++u) {
+              const int zw = z0 + 32 * u;
+              if (zw <= khi)
+                count_window(H, n, lane, zw, min(32, khi - zw + 1), c2[u], c3[u], kmode, kzeq);
+            }
           }
         }
       }
