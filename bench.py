@@ -82,6 +82,10 @@ def parse():
                          "isosceles m=2, squeezed bins; fp32/bf16/bf16x3 vs the FP64 contraction)")
     ap.add_argument("--precision-out", default=None,
                     help="with --precision-study: write the per-bin errors to this JSON file")
+    ap.add_argument("--shard", action="store_true",
+                    help="under torchrun: split every bispectrum's contraction-grid points over "
+                         "the ranks (replicated FFTs, one NCCL all-reduce of the T partial "
+                         "sums); the line reports strong scaling")
     ap.add_argument("--no-studies", action="store_true",
                     help="skip the 512^3 cross precision study and the 1024^3 resident / "
                          "streamed runs that the headline line carries")
@@ -89,6 +93,29 @@ def parse():
                     help="profiling runs only: skip the one-off FP64 grid information and "
                          "normalise by 1 (same kernels and timings in the step)")
     return ap.parse_args()
+
+
+def guarded_leg(name, fn):
+    """Run one extra leg of the bench line; a failure is recorded in the line (and on stderr)
+    instead of losing the headline measurement."""
+    t0 = time.perf_counter()
+    try:
+        out = fn()
+    except Exception as e:  # the headline line must still be printed
+        import traceback
+        traceback.print_exc()
+        out = {"error": "%s: %s" % (type(e).__name__, e)}
+    sys.stderr.write("leg %s: %.1f s\n" % (name, time.perf_counter() - t0))
+    return out
+
+
+def shard_step(plan, tset, ntri, precision, group=None):
+    """One bispectrum split over the process group's ranks: this rank contracts its range of
+    contraction-grid points, the FP64 partial vectors are summed by one all-reduce (bskit's
+    slab sums with gather + bcast, main.py:1875-1879), and every rank normalises."""
+    from bskit_gb300.sharding import sharded_measure_b
+    b = sharded_measure_b(plan, tset, precision=precision, group=group)
+    return plan.normalize(b, ntri)
 
 
 def select_workload(name):
@@ -197,6 +224,9 @@ def run_ours(args):
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
+        sys.stderr.write("rank %d/%d: process group %s on cuda:%d%s\n"
+                         % (rank, world, dist.get_backend(), local,
+                            ", point-range shards" if args.shard else ", replicas"))
     else:
         dist = None
         torch.cuda.set_device(0)
@@ -209,7 +239,9 @@ def run_ours(args):
     edges, tri = workload_bins(args.workload)
     plan = Plan(NMESH, BOX, edges, grid="reduced", device=dev)
     ts = plan.triangles(tri)
-    delta = synthetic.lognormal_mesh_torch(NMESH, BOX, seed=1 + rank, device=dev).contiguous()
+    # replicas measure their own meshes; shards split one mesh's bispectrum
+    seed = 1 if args.shard else 1 + rank
+    delta = synthetic.lognormal_mesh_torch(NMESH, BOX, seed=seed, device=dev).contiguous()
     torch.cuda.synchronize()
 
     # ---- cold: grid information (FP64), once
@@ -227,6 +259,8 @@ def run_ours(args):
 
     def step(p=prec):
         plan.paint(0, delta)
+        if args.shard:  # this rank's point range, then the all-reduce of the T partial sums
+            return shard_step(plan, ts, ntri, p)
         b = plan.measure_b(ts, precision=p)
         return plan.normalize(b, ntri)
 
@@ -259,7 +293,9 @@ def run_ours(args):
     clk = clocks.stop()
     plan.sync_check()
     ms_step = ms / args.steps
-    value = world * args.steps / (ms / 1e3)
+    # replicas: every rank measures its own bispectra; shards: the ranks measure one together
+    per_step = 1 if args.shard else world
+    value = per_step * args.steps / (ms / 1e3)
 
     # ---- end to end through the public API: pinned host mesh in, B to host each step.
     # The host->device copy of step k+1 runs on a copy stream while step k computes
@@ -289,8 +325,11 @@ def run_ours(args):
             free[i].record(stream)
             if k + 1 < n:
                 prefetch(k + 1)
-            b = plan.measure_b(ts, precision=prec)
-            out_host.copy_(plan.normalize(b, ntri), non_blocking=True)
+            if args.shard:
+                out_host.copy_(shard_step(plan, ts, ntri, prec), non_blocking=True)
+            else:
+                b = plan.measure_b(ts, precision=prec)
+                out_host.copy_(plan.normalize(b, ntri), non_blocking=True)
 
     run_e2e(2)
     plan.sync_check()
@@ -307,7 +346,7 @@ def run_ours(args):
         t = torch.tensor([e2e_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    e2e_value = world * args.steps / (e2e_ms / 1e3)
+    e2e_value = per_step * args.steps / (e2e_ms / 1e3)
     host_check = out_host.clone()
 
     # ---- contraction alone (fields and split cached): the dominant kernel
@@ -395,9 +434,9 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_sampled(delta.cpu().numpy(), edges, tri)
-        if args.workload == "mesh512_all":
-            cpu["full_256"] = cpu_full_256(value_256=None)
+        cpu = guarded_leg("cpu_baseline", lambda: cpu_sampled(delta.cpu().numpy(), edges, tri))
+        if args.workload == "mesh512_all" and "error" not in cpu:
+            cpu["full_256"] = guarded_leg("cpu_full_256", cpu_full_256)
 
     line = {
         "metric": METRIC,
@@ -408,7 +447,7 @@ def run_ours(args):
         "warmup": args.warmup,
         "ms_per_step": ms_step,
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": "strong" if args.shard else "weak",
         "vs_baseline": None,
         "dtype": prec,
         "data": "synthetic lognormal mesh (seeded), no dataset",
@@ -417,7 +456,9 @@ def run_ours(args):
                    "n_bins": int(len(tri)), "precision": prec, "contraction_grid": ng,
                    "l2": "inputs larger than L2 (mesh %d MiB, shell fields %.1f GiB)"
                          % (NMESH ** 3 * 4 >> 20, len(edges) * ng ** 3 * 4 / 2 ** 30),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": ("point-range shards of one bispectrum over %d GPUs, NCCL "
+                                   "all-reduce of the T partial sums" % world) if args.shard
+                   else ("replicas" if world > 1 else "single GPU")},
         "e2e": {"value": e2e_value, "unit": "bispectra/s",
                 "h2d_bytes_per_step": int(host.numel() * 4),
                 "d2h_bytes_per_step": int(out_host.numel() * 8),
@@ -448,18 +489,20 @@ def run_ours(args):
         del delta, host, bufs
         torch.cuda.empty_cache()
     if studies:
-        line["precision_study"] = precision_study(args, dev)
-        line["mesh1024"] = mesh1024_study(args, dev)
-        torch.cuda.empty_cache()
+        for key, fn in (("precision_study", precision_study), ("mesh1024", mesh1024_study)):
+            line[key] = guarded_leg(key, lambda fn=fn: fn(args, dev))
+            torch.cuda.empty_cache()
     if args.serve_requests > 0 and world == 1:
         sweep = [float(v) for v in args.serve_sweep.split(",") if v.strip()]
-        line["serving"] = run_serving(args, dev, sweep=sweep)
-        line["serving"]["p99_bound_ms"] = SERVE_P99_BOUND_MS
-        line["serving"]["p99_within_bound"] = bool(
-            line["serving"].get("p99_ms", 1e30) <= SERVE_P99_BOUND_MS)
+        line["serving"] = guarded_leg("serving", lambda: run_serving(args, dev, sweep=sweep))
+        if "error" not in line["serving"]:
+            line["serving"]["p99_bound_ms"] = SERVE_P99_BOUND_MS
+            line["serving"]["p99_within_bound"] = bool(
+                line["serving"].get("p99_ms", 1e30) <= SERVE_P99_BOUND_MS)
         if not args.no_fp32:
             torch.cuda.empty_cache()
-            line["serving_fp32"] = run_serving(args, dev, precision="fp32")
+            line["serving_fp32"] = guarded_leg(
+                "serving_fp32", lambda: run_serving(args, dev, precision="fp32"))
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
@@ -747,11 +790,14 @@ def mesh1024_study(args, dev, steps=5):
     fp0 = probe.footprint()
     probe.close()
     K = ng ** 3
-    sp = Plan(n, box, edges, mem_budget=fp0 + 20 * 16 * K, device=dev)
+    # room for 16-shell streaming buffers (16 bytes per point and shell: three FP32 chunks and
+    # the bf16 split of one), not for the 40 resident shells and their split (20 x 16 K)
+    budget = fp0 + 18 * 16 * K
+    sp = Plan(n, box, edges, mem_budget=budget, device=dev)
     ts2 = sp.triangles(tri)
     streamed, b_str = run(sp, ts2, ntri)
     streamed["chunk_shells"] = sp.stream_chunk()
-    streamed["budget_gb"] = (fp0 + 20 * 16 * K) / 1e9
+    streamed["budget_gb"] = budget / 1e9
     sp.close()
     ok = ntri > 0
     diff = float(((b_str - b_res).abs()[ok]).max() / b_res[ok].abs().max())

@@ -531,6 +531,8 @@ void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int prec
         if (!p->slot[sl].fields) need += field_bytes;
       }
     if (tc && !p->slot[c].split) need += split_elems(p->n_alloc(), p->K) * sizeof(__nv_bfloat16);
+    // the field synthesis' workspace is allocated with the first resident fields
+    if (p->use_synth && !p->synth_ws) need += p->synth_ws_bytes;
     const int64_t held =
         p->stream_C ? (int64_t)p->stream_C * p->K * (12 + (p->stream_tc ? 4 : 0)) : 0;
     if (footprint(p) - held + (int64_t)need > (int64_t)p->mem_budget) {
