@@ -21,12 +21,14 @@
 //  * q1 runs over one octant (q1 >= 0 componentwise), each mode weighted by its number of
 //    sign images (2^{nonzero components}): flipping the sign of a component of all three
 //    vectors maps triangles to triangles and keeps every membership (k_c^2 is unchanged).
-//  * For one q1 a CTA sweeps q2 along z-lines (q2_x, q2_y fixed, one line per thread) over
-//    the half-lens |q2|^2 <= R2, |q1 + q2|^2 <= R2, |q3| <= |q2|; the half-lens is the set
-//    of integer z between bounds computed per line.  Pairs with |q3| < |q2| add 2 to
-//    H[y][z], pairs with |q3| = |q2| add 1, so that F(q1; y, z) = (H[y][z] + H[z][y]) / 2.
-//    Consecutive points of a line with the same membership codes are summed in a register
-//    before their shared-memory atomic.
+//  * For one q1 a CTA sweeps q2 along z-lines (q2_x, q2_y fixed) over the half-lens
+//    |q2|^2 <= R2, |q1 + q2|^2 <= R2, |q3| <= |q2|; the half-lens is the set of integer z
+//    between bounds that the lanes of a warp compute for 32 lines at once.  The warp then
+//    walks each line, every lane on 4 consecutive z (one 4-byte read of the q2 codes, two
+//    of the q3 codes, which run the other way and are read from a z-reversed copy of the
+//    table).  Pairs with |q3| < |q2| add 2 to H[y][z], pairs with |q3| = |q2| add 1, so
+//    that F(q1; y, z) = (H[y][z] + H[z][y]) / 2; a lane's consecutive points with the same
+//    membership codes are summed before their shared-memory atomic.
 //  * After each q1 the CTA folds F into its running sums for the q1's shell run:
 //    G[y >= z] += mult * F and W[y >= z] += mult * F * w(q1), w = |q1| in fixed point with
 //    kFrac fractional bits, split at bit 22 into two limbs, so every batch sum is an exact
@@ -48,7 +50,7 @@ namespace genum {
 
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr int kWin = 4;                            // 32-point windows whose loads overlap
+constexpr int kWin = 2;                            // 128-point windows whose loads overlap
 constexpr int kMaxShells = 64;                     // tables of at most 64 shells
 constexpr int kMaxBatch = 32;                      // octant modes per batch
 constexpr int kFrac = 44;                          // fractional bits of the |q| weights
@@ -98,7 +100,8 @@ __device__ __forceinline__ uint16_t code_of(const uint16_t* __restrict__ table, 
 // Byte codes of the cube [-r, r]^3 (zero outside |q|^2 <= R2); flag[0] is set when a mode
 // lies in more than two shells (not representable: the caller falls back).
 __global__ void cube_codes_kernel(const uint16_t* __restrict__ table, int Ng, int r, int R2,
-                                  uint8_t* __restrict__ cube, int* __restrict__ flag) {
+                                  uint8_t* __restrict__ cube, uint8_t* __restrict__ cube_rev,
+                                  int* __restrict__ flag) {
   const int S = 2 * r + 1;
   const int64_t total = (int64_t)S * S * S;
   const int HN = Ng / 2 + 1;
@@ -117,6 +120,7 @@ __global__ void cube_codes_kernel(const uint16_t* __restrict__ table, int Ng, in
       }
     }
     cube[i] = out;
+    cube_rev[i + (int64_t)(-2 * z)] = out;  // (x, y, -z): z runs the other way
   }
 }
 
@@ -126,34 +130,32 @@ __device__ __forceinline__ void add_run(uint32_t* H, int n, uint32_t c2, uint32_
     for (int z = code_first(c3); z <= code_last(c3); ++z) atomicAdd(&H[y * n + z], cnt);
 }
 
-// One 32-point window of a line: lane l holds the codes of z = zb + l (valid for l < nv).
-// Lanes with equal (code2, code3) in a row form a segment; its first lane adds the
-// segment's count (2 per pair, 1 for the pair with |q3| = |q2|) with one atomic.
-__device__ __forceinline__ void count_window(uint32_t* H, int n, int lane, int zb, int nv,
-                                             uint32_t c2, uint32_t c3, int eq_mode, int z_eq) {
-  const bool valid = lane < nv;
-  const uint32_t key = (valid && (c2 & c3 & 0x80u)) ? ((c2 << 8) | c3) : 0u;
-  const uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, key, 1);
-  const bool start = valid && (lane == 0 || key != prev);
-  const uint32_t starts = __ballot_sync(0xFFFFFFFFu, start);
-  if (start && key) {
-    const uint32_t above = lane == 31 ? 0u : starts >> (lane + 1);
-    const int end = above ? lane + __ffs(above) : nv;
-    const int len = end - lane;
-    uint32_t cnt = 2u * (uint32_t)len;
-    if (eq_mode == 1) {
-      cnt = (uint32_t)len;
-    } else if (eq_mode == 2 && z_eq >= zb + lane && z_eq < zb + end) {
-      cnt -= 1u;
+// Four consecutive points z = zg .. zg + 3 of a line, their q2 and q3 codes in the bytes of
+// w2 and w3: runs of equal (code2, code3) add their count (2 per pair, 1 for the pair with
+// |q3| = |q2|) to H with one atomic per run (points outside [lo, hi] count nothing).
+__device__ __forceinline__ void count_quad(uint32_t* H, int n, int zg, int lo, int hi,
+                                           uint32_t w2, uint32_t w3, int eq_mode, int z_eq) {
+  uint32_t run = 0, cnt = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int z = zg + j;
+    const uint32_t c2 = (w2 >> (8 * j)) & 0xFFu, c3 = (w3 >> (8 * j)) & 0xFFu;
+    const uint32_t key = (z >= lo && z <= hi && (c2 & c3 & 0x80u)) ? ((c2 << 8) | c3) : 0u;
+    if (key != run) {
+      if (run) add_run(H, n, run >> 8, run & 0xFFu, cnt);
+      run = key;
+      cnt = 0;
     }
-    add_run(H, n, key >> 8, key & 0xFFu, cnt);
+    cnt += eq_mode == 1 ? 1u : (eq_mode == 2 && z == z_eq ? 1u : 2u);
   }
+  if (run) add_run(H, n, run >> 8, run & 0xFFu, cnt);
 }
 
 // Dynamic shared memory: G, Whi, Wlo (n (n + 1) / 2 uint64 each), then H (n * n uint32).
 __global__ void __launch_bounds__(kThreads, 2)
     enum_kernel(const Mode* __restrict__ modes, const Batch* __restrict__ batches, int n_batches,
-                int* __restrict__ next_batch, const uint8_t* __restrict__ cube, int r, int R2,
+                int* __restrict__ next_batch, const uint8_t* __restrict__ cube,
+                const uint8_t* __restrict__ cube_rev, int r, int R2,
                 int n, unsigned long long* __restrict__ g_cnt, double* __restrict__ g_w) {
   extern __shared__ unsigned long long smem_u64[];
   __shared__ int s_batch;
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(kThreads, 2)
               }
             }
             b2 = ((x2 + r) * S + (y2 + r)) * S + r;        // cube index of (x2, y2, z) - z
-            b3 = ((x3 + r) * S + (y3 + r)) * S + r - z1;   // cube index of q3 + z
+            b3 = ((x3 + r) * S + (y3 + r)) * S + r + z1;   // cube_rev index of q3 - z
           }
         }
         uint32_t todo = __ballot_sync(0xFFFFFFFFu, lo <= hi);
@@ -223,20 +225,27 @@ __global__ void __launch_bounds__(kThreads, 2)
           const int kb3 = __shfl_sync(0xFFFFFFFFu, b3, k);
           const int kmode = __shfl_sync(0xFFFFFFFFu, eq_mode, k);
           const int kzeq = __shfl_sync(0xFFFFFFFFu, z_eq, k);
-          for (int z0 = klo; z0 <= khi; z0 += 32 * kWin) {
-            // every window's loads before any window's counting: kWin L2 round trips overlap
-            uint32_t c2[kWin], c3[kWin];
+          // lane l takes the 4 points zs + 128 u + 4 l .. + 3; zs makes the q2 reads 4-byte
+          // aligned, the q3 reads (the other direction, in cube_rev) are two aligned words
+          // and a funnel shift by the line's offset
+          const int zs = klo - ((kb2 + klo) & 3);
+          const int m3 = (kb3 + zs) & 3;
+          for (int z0 = zs; z0 <= khi; z0 += 128 * kWin) {
+            uint32_t w2[kWin], w3[kWin];
 #pragma unroll
             for (int u = 0; u < kWin; ++u) {
-              const int z = z0 + 32 * u + lane;
-              c2[u] = z <= khi ? __ldg(cube + kb2 + z) : 0u;
-              c3[u] = z <= khi ? __ldg(cube + kb3 - z) : 0u;
+              const int zg = z0 + 128 * u + 4 * lane;
+              w2[u] = w3[u] = 0u;
+              if (zg <= khi) {
+                w2[u] = __ldg(reinterpret_cast<const uint32_t*>(cube + kb2 + zg));
+                const uint32_t* p3 = reinterpret_cast<const uint32_t*>(cube_rev + kb3 + zg - m3);
+                w3[u] = __funnelshift_r(__ldg(p3), __ldg(p3 + 1), 8 * m3);
+              }
             }
 #pragma unroll
             for (int u = 0; u < kWin; ++u) {
-              const int zw = z0 + 32 * u;
-              if (zw <= khi)
-                count_window(H, n, lane, zw, min(32, khi - zw + 1), c2[u], c3[u], kmode, kzeq);
+              const int zg = z0 + 128 * u + 4 * lane;
+              if (zg <= khi) count_quad(H, n, zg, klo, khi, w2[u], w3[u], kmode, kzeq);
             }
           }
         }
@@ -325,19 +334,24 @@ void gridinfo_enum(bsk_plan* p, const std::vector<HostTriangle>& tri, double* nt
   const size_t n_cube = (size_t)S * S * S;
   // byte codes of the cube [-r, r]^3, kept on the device for the enumeration; the octant
   // part is read back to list the q1 modes
+  // [pad][cube][pad][cube_rev][pad][flag]: the pads hold the few bytes that the 4-byte reads
+  // of a line's first and last points take from before and after the cube
+  const size_t pad = 64, span = (n_cube + 15) / 16 * 16;
   char* cube_mem = nullptr;
-  BSK_CHECK_CUDA(cudaMallocAsync((void**)&cube_mem, n_cube + 256, st));
+  BSK_CHECK_CUDA(cudaMallocAsync((void**)&cube_mem, 3 * pad + 2 * span + 16, st));
   struct FreeCube {
     char* w;
     cudaStream_t s;
     ~FreeCube() { cudaFreeAsync(w, s); }
   } free_cube{cube_mem, st};
-  uint8_t* d_cube = (uint8_t*)cube_mem;
-  int* d_flag = (int*)(cube_mem + (n_cube + 15) / 16 * 16);
+  BSK_CHECK_CUDA(cudaMemsetAsync(cube_mem, 0, 3 * pad + 2 * span + 16, st));
+  uint8_t* d_cube = (uint8_t*)cube_mem + pad;
+  uint8_t* d_cube_rev = d_cube + span + pad;
+  int* d_flag = (int*)(d_cube_rev + span + pad);
   std::vector<uint8_t> cube(n_cube);
   int flag = 0;
-  BSK_CHECK_CUDA(cudaMemsetAsync(d_flag, 0, sizeof(int), st));
-  cube_codes_kernel<<<p->num_sms * 8, 256, 0, st>>>(p->table, p->Ng, r, R2, d_cube, d_flag);
+  cube_codes_kernel<<<p->num_sms * 8, 256, 0, st>>>(p->table, p->Ng, r, R2, d_cube, d_cube_rev,
+                                                    d_flag);
   BSK_CHECK_CUDA(cudaGetLastError());
   BSK_CHECK_CUDA(cudaMemcpyAsync(cube.data(), d_cube, n_cube, cudaMemcpyDeviceToHost, st));
   BSK_CHECK_CUDA(cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -405,7 +419,7 @@ void gridinfo_enum(bsk_plan* p, const std::vector<HostTriangle>& tri, double* nt
                                                                  smem));
     const int grid = std::max(1, std::min<int>((int)batches.size(), per_sm * p->num_sms));
     enum_kernel<<<grid, kThreads, smem, st>>>(d_modes, d_batches, (int)batches.size(), d_next,
-                                              d_cube, r, R2, n, g_cnt, g_w);
+                                              d_cube, d_cube_rev, r, R2, n, g_cnt, g_w);
     BSK_CHECK_CUDA(cudaGetLastError());
   }
   const double kf = 2.0 * 3.14159265358979323846 / p->L;
