@@ -154,11 +154,26 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// try_wait with a suspend-time hint: the thread sleeps in hardware until the phase completes
+// or about `ns` nanoseconds pass, instead of returning after the system's default limit.
+__device__ __forceinline__ bool mbar_try_sleep(uint64_t* bar, uint32_t parity, uint32_t ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.b32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+constexpr uint32_t kSuspendNs = 20000;  // a waiting warp issues no instructions meanwhile
 // Bounded wait: false when the wait expired or another role already gave up.
-// mbarrier.try_wait suspends the thread in hardware for a while, so the loop
-// is cheap; the clock is read every 16 polls and global memory (the shared
-// error flag, the wall clock) only about every 2^20 cycles, so that no memory
-// round trip sits between a barrier's completion and the waiter seeing it.
+// mbarrier.try_wait suspends the thread in hardware (up to kSuspendNs, or until the phase
+// completes), so a waiting warp takes few issue slots from the working ones; the clock is
+// read every 16 polls and global memory (the shared error flag, the wall clock) only about
+// every 2^20 cycles, so that no memory round trip sits between a barrier's completion and
+// the waiter seeing it.
 __device__ __noinline__ bool mbar_wait_slow(uint64_t* bar, uint32_t parity) {
   if (mbar_try(bar, parity)) return true;
   long long c0 = clock64();
@@ -166,7 +181,7 @@ __device__ __noinline__ bool mbar_wait_slow(uint64_t* bar, uint32_t parity) {
   while (true) {
 #pragma unroll 1
     for (int i = 0; i < 16; ++i)
-      if (mbar_try(bar, parity)) return true;
+      if (mbar_try_sleep(bar, parity, kSuspendNs)) return true;
     const long long c = clock64();
     if (c - c0 > (1ll << 20)) {
       c0 = c;

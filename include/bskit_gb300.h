@@ -16,8 +16,9 @@
  *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
  *    Work is enqueued on that stream; the host does not synchronise except
  *    in bsk_plan_create / bsk_triset_create / bsk_shell_mode_counts /
- *    bsk_compensate_cic / bsk_sync_check / bsk_contract_noalloc (which waits
- *    for its own schedule copies on `stream` and so cannot be captured).
+ *    bsk_compensate_cic / bsk_sync_check / bsk_gridinfo (enumeration path) /
+ *    bsk_contract_noalloc (which waits for its own schedule copies on `stream`
+ *    and so cannot be captured).
  *  - A plan is bound to the CUDA device that was current at creation.
  *    Calls on one plan must be serialised by the caller; distinct plans may
  *    run on distinct streams concurrently.
@@ -201,9 +202,14 @@ int bsk_measure_b_range(bsk_plan* plan, const bsk_triset* set, int slot_a, int s
                         double* b_unnorm, void* stream);
 
 /*
- * Grid information of every triangle: ntri[t] = exact triangle count
- * (rounded FP64 sum), kmean[3t+a] = mean |k_a| over the bin's triangles
- * (NaN when ntri == 0).  FP64 fields, FP64 contraction.
+ * Grid information of every triangle: ntri[t] = exact triangle count,
+ * kmean[3t+a] = mean |k_a| over the bin's triangles (NaN when ntri == 0).
+ * When no triangle of shell modes can wrap around the grid (grid side above
+ * three times the largest |q_c| of a shell mode: every reduced plan) and the
+ * plan has at most 64 shells, the sums are evaluated exactly by enumerating
+ * the lattice triangles q1 + q2 + q3 = 0 (integer counts, fixed-point |q|
+ * sums); otherwise from FP64 indicator / |k| fields and an FP64 contraction
+ * (counts are the rounded FP64 sums).  The enumeration synchronises `stream`.
  * Replaces: FFTBispectrum.measure_gridinfo_faster, bskit/main.py:1941-2132,
  *           compute_Nbin / compute_k_means_on_grid, main.py:431-567.
  */
