@@ -21,14 +21,16 @@
 //     round-to-nearest) and store them with tcgen05.st into the 2-stage TMEM
 //     A-operand ring (lane = GEMM row);
 //   * warp 1 runs the stage loop and one elected lane issues, per 16-point K step,
-//     tcgen05.mma kind::f16 with A from TMEM and B from SMEM: hi x Bhi and, for
-//     bf16x3, hi x Blo and lo x Bhi, all three into the same nc accumulator columns
-//     (N = nc rounded up to the MMA's multiple of 16; the extra columns are never read).  The tensor core's FP32 accumulate
+//     tcgen05.mma kind::f16 with A from TMEM and B from SMEM: hi x [Bhi; Blo]
+//     (N = 2 nc: one MMA yields both hi*Bhi and hi*Blo) and, for bf16x3, lo x Bhi
+//     (N = nc rounded up to the MMA's multiple of 16, into the hi*Bhi columns; when
+//     nc is an odd multiple of 8 the last 8 of those N columns are lo x Blo of the
+//     first 8 column shells, landing on their hi*Blo sums: an extra, exact term).  The tensor core's FP32 accumulate
 //     truncates, so an accumulator is only ever fed one stage (16 MMAs) before it is
 //     handed over;
 //   * warps 2..9 (2 per lane quadrant, 32 columns each) drain each finished
-//     accumulator with tcgen05.ld (one load per 16 columns: the three products
-//     already summed), add it into per-thread FP32 registers (round-to-nearest), and at the end
+//     accumulator with tcgen05.ld (hi*B + lo*Bhi columns and hi*Blo columns),
+//     add it into per-thread FP32 registers (round-to-nearest), and at the end
 //     of the slice add the entries that are triangle bins into the FP64 output
 //     (atomics).
 // The MMAs' completion is committed once per stage, to a ring of mbarriers that
@@ -62,7 +64,7 @@ constexpr int AGW = 4;
 constexpr int NUM_WARPS = 10 + 4 * AGW;       // producer, MMA, 8 drain, 4 AGW A-operand
 constexpr int THREADS = NUM_WARPS * 32;
 constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t ACC_COL = 0;               // accumulator b at 128 b: [0, nc) hi*Bhi + hi*Blo + lo*Bhi
+constexpr uint32_t ACC_COL = 0;               // accumulator b at 128 b: [0,nc) hi*Bhi+lo*Bhi, [nc,2nc) hi*Blo
 constexpr uint32_t A_COL = 256;               // A stage a at 256 + 128 a: hi +0..63, lo +64..127
 // Points per work item: 32 768 when that still gives every SM at least kMinItemsPerSm
 // items (one CTA per SM walks them), else 16 384.  Longer slices spread the per-item
@@ -154,26 +156,11 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// try_wait with a suspend-time hint: the thread sleeps in hardware until the phase completes
-// or about `ns` nanoseconds pass, instead of returning after the system's default limit.
-__device__ __forceinline__ bool mbar_try_sleep(uint64_t* bar, uint32_t parity, uint32_t ns) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-      "selp.b32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
-      : "memory");
-  return ok != 0;
-}
-constexpr uint32_t kSuspendNs = 20000;  // a waiting warp issues no instructions meanwhile
 // Bounded wait: false when the wait expired or another role already gave up.
-// mbarrier.try_wait suspends the thread in hardware (up to kSuspendNs, or until the phase
-// completes), so a waiting warp takes few issue slots from the working ones; the clock is
-// read every 16 polls and global memory (the shared error flag, the wall clock) only about
-// every 2^20 cycles, so that no memory round trip sits between a barrier's completion and
-// the waiter seeing it.
+// mbarrier.try_wait suspends the thread in hardware for a while, so the loop
+// is cheap; the clock is read every 16 polls and global memory (the shared
+// error flag, the wall clock) only about every 2^20 cycles, so that no memory
+// round trip sits between a barrier's completion and the waiter seeing it.
 __device__ __noinline__ bool mbar_wait_slow(uint64_t* bar, uint32_t parity) {
   if (mbar_try(bar, parity)) return true;
   long long c0 = clock64();
@@ -181,7 +168,7 @@ __device__ __noinline__ bool mbar_wait_slow(uint64_t* bar, uint32_t parity) {
   while (true) {
 #pragma unroll 1
     for (int i = 0; i < 16; ++i)
-      if (mbar_try_sleep(bar, parity, kSuspendNs)) return true;
+      if (mbar_try(bar, parity)) return true;
     const long long c = clock64();
     if (c - c0 > (1ll << 20)) {
       c0 = c;
@@ -467,14 +454,13 @@ __global__ void __launch_bounds__(THREADS, 1)
       const TileDesc td = tiles[item % n_tiles];
       const int64_t x_begin = k_begin + sl * slice;
       const int64_t x_end = min(k_end, x_begin + slice);
-      // hi x Bhi, hi x Blo (the lo rows of a block follow its nc hi rows) and lo x Bhi, all
-      // into accumulator columns [0, nc), so that the drain reads each sum once.  N is a
-      // multiple of 16: with nc an odd multiple of 8 the MMAs also cover 8 more B rows
-      // (within the stage's B region), whose columns [nc, nc + 8) the drain never reads.
+      // hi x [Bhi; Blo] (the lo rows of a block sit right after its nc hi rows), lo x Bhi.
+      // N is a multiple of 16: an N = nc MMA with nc an odd multiple of 8 also covers the
+      // first 8 lo rows (accumulated into hi*Blo columns the drain adds anyway, or never read)
       const int n16 = (td.nc + 15) & ~15;
       const uint32_t kb_bytes = 2u * td.nc * 128u;
-      const uint32_t lo_bytes = td.nc * 128u;
-      const uint32_t idesc = idesc_bf16(n16);
+      const uint32_t idesc_stack = idesc_bf16(terms >= 3 ? 2 * td.nc : n16);
+      const uint32_t idesc_hi = idesc_bf16(n16);
       for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
         // a fresh accumulator per stage, once the drain has emptied it
         const uint32_t b = grp % NACC;
@@ -497,13 +483,9 @@ __global__ void __launch_bounds__(THREADS, 1)
           uint32_t accum = 0;
 #pragma unroll
           for (int k = 0; k < KCH / 16; ++k) {
-            const uint32_t b_hi = st + (k >> 2) * kb_bytes + 32 * (k & 3);
-            const uint64_t bdesc = desc_sw128(b_hi);
-            mma_ts(d_tmem, a_hi + 8 * k, bdesc, idesc, accum);
-            if (terms >= 3) {
-              mma_ts(d_tmem, a_hi + 8 * k, desc_sw128(b_hi + lo_bytes), idesc, 1);
-              mma_ts(d_tmem, a_lo + 8 * k, bdesc, idesc, 1);
-            }
+            const uint64_t bdesc = desc_sw128(st + (k >> 2) * kb_bytes + 32 * (k & 3));
+            mma_ts(d_tmem, a_hi + 8 * k, bdesc, idesc_stack, accum);
+            if (terms >= 3) mma_ts(d_tmem, a_lo + 8 * k, bdesc, idesc_hi, 1);
             accum = 1;
           }
           tc_commit(&bars->done[chunk % DONE_RING]);
@@ -550,6 +532,11 @@ __global__ void __launch_bounds__(THREADS, 1)
             tmem_ld16(taddr + ACC_COL + b * 128 + cc * 16, v);
 #pragma unroll
             for (int e = 0; e < 16; ++e) acc[cc * 16 + e] += __uint_as_float(v[e]);
+            if (terms >= 3) {
+              tmem_ld16(taddr + ACC_COL + b * 128 + td.nc + cc * 16, v);
+#pragma unroll
+              for (int e = 0; e < 16; ++e) acc[cc * 16 + e] += __uint_as_float(v[e]);
+            }
           }
         }
         tc_fence_before();
