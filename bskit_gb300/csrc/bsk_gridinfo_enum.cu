@@ -18,21 +18,24 @@
 //   N_tri(x, y, z) = sum_{q1 in x} F(q1; y, z),   S(x; y, z) = sum_{q1 in x} |q1| F(q1; y, z)
 // and, by relabelling the triangle, sum |q2| of bin (a, b, c) = S(b; a, c) and sum |q3| =
 // S(c; a, b); F is symmetric in (y, z).
-//  * q1 runs over one octant (q1 >= 0 componentwise), each mode weighted by its number of
-//    sign images (2^{nonzero components}): flipping the sign of a component of all three
-//    vectors maps triangles to triangles and keeps every membership (k_c^2 is unchanged).
+//  * q1 runs over x >= y >= 0, z >= 0, each mode weighted by the size of its orbit under
+//    sign flips and the x <-> y swap (2^{nonzero components}, times 2 when x != y): applied
+//    to all three vectors these map triangles to triangles and keep every membership, since
+//    k_c^2 does not change under a sign flip and (kx*kx + ky*ky) is the same sum either
+//    way (floating-point addition commutes).  z is not swapped with x or y: it is added last,
+//    and at edge ties the rounded sum depends on that order.
 //  * For one q1 a CTA sweeps q2 along z-lines (q2_x, q2_y fixed) over the half-lens
 //    |q2|^2 <= R2, |q1 + q2|^2 <= R2, |q3| <= |q2|; the half-lens is the set of integer z
 //    between bounds that the lanes of a warp compute for 32 lines at once.  The warp then
-//    walks each line, every lane on 4 consecutive z (one 4-byte read of the q2 codes, two
-//    of the q3 codes, which run the other way and are read from a z-reversed copy of the
-//    table).  Pairs with |q3| < |q2| add 2 to H[y][z], pairs with |q3| = |q2| add 1, so
-//    that F(q1; y, z) = (H[y][z] + H[z][y]) / 2; a lane's consecutive points with the same
-//    membership codes are summed before their shared-memory atomic.
+//    walks those lines as one packed stream of 8-point groups, a group per lane (one 8-byte
+//    read of the q2 codes, two of the q3 codes, which run the other way and are read from a
+//    z-reversed copy of the table).  Pairs with |q3| < |q2| add 2 to H[y][z], pairs with
+//    |q3| = |q2| add 1, so that F(q1; y, z) = (H[y][z] + H[z][y]) / 2; lanes whose points
+//    have the same membership codes add their counts with one shared-memory atomic.
 //  * After each q1 the CTA folds F into its running sums for the q1's shell run:
 //    G[y >= z] += mult * F and W[y >= z] += mult * F * w(q1), w = |q1| in fixed point with
 //    kFrac fractional bits, split at bit 22 into two limbs, so every batch sum is an exact
-//    integer in uint64 (for |q| < 256: per-mode counts below 2^28 with the sign images,
+//    integer in uint64 (for |q| < 256: per-mode counts below 2^29 with the orbit weights,
 //    limbs below 2^30 and 2^22, kMaxBatch modes per batch).
 //  * A batch is at most kMaxBatch octant modes of one membership run; at its end the CTA adds
 //    its counts to the global uint64 table and its |q| sums, converted to FP64, to the
@@ -50,7 +53,6 @@ namespace genum {
 
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr int kWin = 2;                            // 128-point windows whose loads overlap
 constexpr int kMaxShells = 64;                     // tables of at most 64 shells
 constexpr int kMaxBatch = 32;                      // octant modes per batch
 constexpr int kFrac = 44;                          // fractional bits of the |q| weights
@@ -130,25 +132,60 @@ __device__ __forceinline__ void add_run(uint32_t* H, int n, uint32_t c2, uint32_
     for (int z = code_first(c3); z <= code_last(c3); ++z) atomicAdd(&H[y * n + z], cnt);
 }
 
-// Four consecutive points z = zg .. zg + 3 of a line, their q2 and q3 codes in the bytes of
-// w2 and w3: runs of equal (code2, code3) add their count (2 per pair, 1 for the pair with
-// |q3| = |q2|) to H with one atomic per run (points outside [lo, hi] count nothing).
-__device__ __forceinline__ void count_quad(uint32_t* H, int n, int zg, int lo, int hi,
-                                           uint32_t w2, uint32_t w3, int eq_mode, int z_eq) {
-  uint32_t run = 0, cnt = 0;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int z = zg + j;
-    const uint32_t c2 = (w2 >> (8 * j)) & 0xFFu, c3 = (w3 >> (8 * j)) & 0xFFu;
-    const uint32_t key = (z >= lo && z <= hi && (c2 & c3 & 0x80u)) ? ((c2 << 8) | c3) : 0u;
-    if (key != run) {
-      if (run) add_run(H, n, run >> 8, run & 0xFFu, cnt);
-      run = key;
-      cnt = 0;
-    }
-    cnt += eq_mode == 1 ? 1u : (eq_mode == 2 && z == z_eq ? 1u : 2u);
+// Bits 7, 15, 23, 31 of m (and no others) -> bits 0..3.  The multiplier moves bit 8j + 7 to
+// bit 28 + j; every other product term lands outside bits 24..31 (8j - 7k is distinct for
+// j, k in 0..3), so no carry reaches them.
+__device__ __forceinline__ uint32_t high_bits4(uint32_t m) { return (m * 0x00204081u) >> 28; }
+
+// 0x80 in each byte of x that is zero (the per-byte carry stays inside its byte).
+__device__ __forceinline__ uint32_t zero_bytes(uint32_t x) {
+  return ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u;
+}
+
+// The warp's 256 points of one iteration of the packed line stream: lane l holds the 8
+// consecutive points zg .. zg + 7 of one line, their q2 and q3 codes in the bytes of w2 and
+// (w3lo, w3hi), and in8: which of them count (inside the line's z-interval, both codes
+// valid).  A run is a maximal stretch of counted points of the stream with equal (code2,
+// code3); runs may cross lanes (neighbouring lanes hold neighbouring groups, mostly of one
+// line) and even lines, which only merges counts of one (y, z) bin.  The lane holding a
+// run's first point adds 2 per point of the run to H with one atomic (pairs with
+// |q3| = |q2| are corrected per line by the caller).
+__device__ __forceinline__ void count_group(uint32_t* H, int n, int lane, uint32_t in8,
+                                            uint2 w2, uint32_t w3lo, uint32_t w3hi) {
+  // the previous point of the stream: its two codes and whether it counts
+  uint32_t prev = __shfl_up_sync(
+      0xFFFFFFFFu, (__byte_perm(w2.y, w3hi, 0x3700) & 0xFFFF0000u) | (in8 >> 7), 1);
+  if (lane == 0) prev = 0u;
+  // codes shifted by one point: byte i holds point i - 1's code
+  const uint32_t p2lo = __funnelshift_l(prev, w2.x, 8), p3lo = __byte_perm(prev, w3lo, 0x6542);
+  const uint32_t p2hi = __funnelshift_l(w2.x, w2.y, 8), p3hi = __funnelshift_l(w3lo, w3hi, 8);
+  const uint32_t same8 = high_bits4(zero_bytes((w2.x ^ p2lo) | (w3lo ^ p3lo))) |
+                         (high_bits4(zero_bytes((w2.y ^ p2hi) | (w3hi ^ p3hi))) << 4);
+  const uint32_t prev_in8 = ((in8 << 1) | (prev & 1u)) & 0xFFu;
+  const uint32_t st8 = in8 & ~(same8 & prev_in8);  // run starts
+  const uint32_t brk = st8 | (~in8 & 0xFFu);       // points where no run continues
+  const uint32_t brk_lanes = __ballot_sync(0xFFFFFFFFu, brk != 0u);
+  // the end of a run that no later point of this lane ends: the first break of a later
+  // lane (position 256 when none)
+  const uint32_t later = brk_lanes & (lane == 31 ? 0u : ~((2u << lane) - 1u));
+  const int nl = later ? __ffs(later) - 1 : 32;
+  const uint32_t nbrk = __shfl_sync(0xFFFFFFFFu, brk, nl & 31);
+  const int far_pos = nl < 32 ? 8 * nl + __ffs(nbrk) - 1 : 256;
+  uint32_t s8 = st8;
+  while (s8) {
+    const int j = __ffs(s8) - 1;
+    s8 &= s8 - 1;
+    const uint32_t after = brk >> (j + 1);
+    const int s_pos = 8 * lane + j;
+    const int e_pos = after ? s_pos + __ffs(after) : far_pos;
+    const uint32_t cnt = 2u * (uint32_t)(e_pos - s_pos);
+    const uint32_t c2 = __byte_perm(w2.x, w2.y, j) & 0xFFu;
+    const uint32_t c3 = __byte_perm(w3lo, w3hi, j) & 0xFFu;
+    if (((c2 | c3) & 0x40u) == 0u)  // both points in one shell: code = 0x80 | shell
+      atomicAdd(&H[(int)(c2 * n + c3) - 0x80 * (n + 1)], cnt);
+    else
+      add_run(H, n, c2, c3, cnt);
   }
-  if (run) add_run(H, n, run >> 8, run & 0xFFu, cnt);
 }
 
 // Dynamic shared memory: G, Whi, Wlo (n (n + 1) / 2 uint64 each), then H (n * n uint32).
@@ -215,45 +252,77 @@ __global__ void __launch_bounds__(kThreads, 2)
             b3 = ((x3 + r) * S + (y3 + r)) * S + r + z1;   // cube_rev index of q3 - z
           }
         }
-        uint32_t todo = __ballot_sync(0xFFFFFFFFu, lo <= hi);
-        while (todo) {
-          const int k = __ffs(todo) - 1;
-          todo &= todo - 1;
-          const int klo = __shfl_sync(0xFFFFFFFFu, lo, k);
-          const int khi = __shfl_sync(0xFFFFFFFFu, hi, k);
-          const int kb2 = __shfl_sync(0xFFFFFFFFu, b2, k);
-          const int kb3 = __shfl_sync(0xFFFFFFFFu, b3, k);
-          const int kmode = __shfl_sync(0xFFFFFFFFu, eq_mode, k);
-          const int kzeq = __shfl_sync(0xFFFFFFFFu, z_eq, k);
-          // lane l takes the 4 points zs + 128 u + 4 l .. + 3; zs makes the q2 reads 4-byte
-          // aligned, the q3 reads (the other direction, in cube_rev) are two aligned words
-          // and a funnel shift by the line's offset
-          const int zs = klo - ((kb2 + klo) & 3);
-          const int m3 = (kb3 + zs) & 3;
-          for (int z0 = zs; z0 <= khi; z0 += 128 * kWin) {
-            uint32_t w2[kWin], w3[kWin];
-#pragma unroll
-            for (int u = 0; u < kWin; ++u) {
-              const int zg = z0 + 128 * u + 4 * lane;
-              w2[u] = w3[u] = 0u;
-              if (zg <= khi) {
-                w2[u] = __ldg(reinterpret_cast<const uint32_t*>(cube + kb2 + zg));
-                const uint32_t* p3 = reinterpret_cast<const uint32_t*>(cube_rev + kb3 + zg - m3);
-                w3[u] = __funnelshift_r(__ldg(p3), __ldg(p3 + 1), 8 * m3);
-              }
-            }
-#pragma unroll
-            for (int u = 0; u < kWin; ++u) {
-              const int zg = z0 + 128 * u + 4 * lane;
-              if (zg <= khi) count_quad(H, n, zg, klo, khi, w2[u], w3[u], kmode, kzeq);
-            }
+        // The stream below counts 2 for every pair; the pairs with |q3| = |q2| count once:
+        // the point z_eq of an eq_mode 2 line, every point of an eq_mode 1 line (z1 = 0, rare)
+        if (eq_mode == 2 && z_eq >= lo && z_eq <= hi) {
+          const uint32_t c2 = cube[b2 + z_eq], c3 = cube_rev[b3 + z_eq];
+          if (c2 & c3 & 0x80u) add_run(H, n, c2, c3, 0xFFFFFFFFu);
+        } else if (eq_mode == 1) {
+          for (int z = lo; z <= hi; ++z) {
+            const uint32_t c2 = cube[b2 + z], c3 = cube_rev[b3 + z];
+            if (c2 & c3 & 0x80u) add_run(H, n, c2, c3, 0xFFFFFFFFu);
           }
+        }
+        // The block's lines as one stream of 8-point groups: line k (lane k's) has g_k
+        // groups from zs_k (zs_k <= lo_k, q2 reads 8-byte aligned); lane l of an iteration
+        // takes group t = t0 + l, whose line it finds by a binary search over the inclusive
+        // prefix sums of g, and whose points start at zg = base_k + 8 t.
+        const int zs = lo - ((b2 + lo) & 7);
+        const int g = lo <= hi ? (hi - zs) / 8 + 1 : 0;
+        int incl = g;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const int v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+          if (lane >= d) incl += v;
+        }
+        const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        const int base = zs - 8 * (incl - g);
+        const int a2 = b2 + base, a3 = b3 + base, zlo = lo - base, zhi = hi - base;
+        for (int t0 = 0; t0 < total; t0 += 32) {
+          const int t = t0 + lane;
+          int k = 0;  // the number of lines whose groups all come before t
+#pragma unroll
+          for (int step = 16; step >= 1; step >>= 1)
+            if (__shfl_sync(0xFFFFFFFFu, incl, k + step - 1) <= t) k += step;
+          const bool valid = t < total;
+          k = min(k, 31);
+          const int o = 8 * t;
+          const int ka2 = __shfl_sync(0xFFFFFFFFu, a2, k) + o;
+          const int ka3 = __shfl_sync(0xFFFFFFFFu, a3, k) + o;
+          const int klo = __shfl_sync(0xFFFFFFFFu, zlo, k) - o;
+          const int khi = __shfl_sync(0xFFFFFFFFu, zhi, k) - o;
+          uint2 w2 = make_uint2(0u, 0u);
+          uint32_t w3lo = 0u, w3hi = 0u, in8 = 0u;
+          if (valid) {
+            w2 = __ldg(reinterpret_cast<const uint2*>(cube + ka2));
+            // q3's codes run the other way: read from cube_rev, 16 aligned bytes and funnel
+            // shifts by the group's offset
+            const int m3 = ka3 & 7;
+            const uint2* p3 = reinterpret_cast<const uint2*>(cube_rev + ka3 - m3);
+            const uint2 x = __ldg(p3), y = __ldg(p3 + 1);
+            const int sh = 8 * (m3 & 3);
+            if (m3 < 4) {
+              w3lo = __funnelshift_r(x.x, x.y, sh);
+              w3hi = __funnelshift_r(x.y, y.x, sh);
+            } else {
+              w3lo = __funnelshift_r(x.y, y.x, sh);
+              w3hi = __funnelshift_r(y.x, y.y, sh);
+            }
+            // points lo - zg .. hi - zg of the group (the first group starts at most 7 before
+            // lo, every group starts at or before hi), with both codes valid
+            const int za = max(klo, 0), zb = min(khi, 7);
+            const uint32_t ok8 = high_bits4(w2.x & w3lo & 0x80808080u) |
+                                 (((w2.y & w3hi & 0x80808080u) * 0x00204081u) >> 24);
+            in8 = ok8 & (0xFFu << za) & (0xFFu >> (7 - zb));
+          }
+          count_group(H, n, lane, in8, w2, w3lo, w3hi);
         }
       }
       __syncthreads();
       // fold F(q1; y, z) = (H[y][z] + H[z][y]) / 2 into the batch sums, weighted by the
       // mode's sign images and its fixed-point |q1|
-      const unsigned long long mult = 1ull << ((x1 != 0) + (y1 != 0) + (z1 != 0));
+      const unsigned long long mult = (1ull << ((x1 != 0) + (y1 != 0) + (z1 != 0)))
+                                      << (x1 != y1 ? 1 : 0);
       const unsigned long long w_hi = q1.w >> kLimb, w_lo = q1.w & ((1ull << kLimb) - 1);
       for (int i = threadIdx.x; i < n * n; i += kThreads) {
         const int y = i / n, z = i - y * n;
@@ -359,7 +428,7 @@ void gridinfo_enum(bsk_plan* p, const std::vector<HostTriangle>& tri, double* nt
   BSK_REQUIRE(flag == 0, BSK_ERR_STATE, "internal: a mode lies in more than two shells");
   std::vector<Mode> modes;
   for (int x = 0; x <= r; ++x)
-    for (int y = 0; y <= r; ++y)
+    for (int y = 0; y <= x; ++y)  // x >= y: the x <-> y swap is a symmetry too
       for (int z = 0; z <= r; ++z) {
         const uint8_t c = cube[((size_t)(x + r) * S + (y + r)) * S + (z + r)];
         if (c & 0x80) {
@@ -370,12 +439,12 @@ void gridinfo_enum(bsk_plan* p, const std::vector<HostTriangle>& tri, double* nt
       }
   std::stable_sort(modes.begin(), modes.end(),
                    [](const Mode& a, const Mode& b) { return a.code < b.code; });
-  // a mode adds at most 8 * (largest shell count) * 2^30 to a high-limb sum: the batch is
+  // a mode adds at most 16 * (largest shell count) * 2^30 to a high-limb sum: the batch is
   // short enough that kMaxBatch such terms stay below 2^63
   int64_t max_count = 1;
   for (int64_t c : p->counts) max_count = std::max(max_count, c);
   const size_t batch_len = (size_t)std::max<int64_t>(
-      1, std::min<int64_t>(kMaxBatch, (INT64_MAX >> 33) / max_count));
+      1, std::min<int64_t>(kMaxBatch, (INT64_MAX >> 34) / max_count));
   std::vector<Batch> batches;
   for (size_t i = 0; i < modes.size();) {
     size_t j = i;
