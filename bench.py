@@ -56,7 +56,7 @@ WORKLOAD = WORKLOADS["mesh512_all"][4]
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16x3")
@@ -105,6 +105,13 @@ def guarded_leg(name, fn):
         import traceback
         traceback.print_exc()
         out = {"error": "%s: %s" % (type(e).__name__, e)}
+    # release what the leg left behind before the next leg sizes its memory
+    import gc
+    gc.collect()
+    if "torch" in sys.modules:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.empty_cache()
     sys.stderr.write("leg %s: %.1f s\n" % (name, time.perf_counter() - t0))
     return out
 
@@ -151,7 +158,13 @@ def measured_peaks():
 
 
 class ClockSampler(object):
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region.
+
+    start() launches the sampler and waits (up to 5 s) for its first row, so that the timed
+    region that follows is covered from its beginning; mark() records where the timed region
+    begins; stop() keeps the rows taken after the mark.  A region shorter than one sampling
+    interval has no row of its own: the row just before it is reported, with
+    "samples_in_region": 0."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -161,6 +174,16 @@ class ClockSampler(object):
         self.gpu = gpu_index
         self.proc = None
         self.path = None
+        self.mark_rows = 0
+
+    def _rows(self):
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        return rows
 
     def start(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
@@ -172,6 +195,13 @@ class ClockSampler(object):
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        t0 = time.time()
+        while time.time() - t0 < 5.0 and not self._rows() and self.proc.poll() is None:
+            time.sleep(0.05)
+
+    def mark(self):
+        self.mark_rows = len(self._rows()) if self.proc is not None else 0
 
     def stop(self):
         if self.proc is None:
@@ -181,25 +211,25 @@ class ClockSampler(object):
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        rows = []
-        with open(self.path) as f:
-            for line in f:
-                parts = [p.strip() for p in line.split(",")]
-                if len(parts) >= 9:
-                    rows.append(parts)
+        rows = self._rows()
         os.unlink(self.path)
         if not rows:
             return None
-        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        inside = rows[self.mark_rows:]
+        n_inside = len(inside)
+        if not inside:
+            inside = rows[-1:]
+        sm = sorted(float(r[1]) for r in inside if r[1].replace(".", "").isdigit())
         reasons = set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
+        for r in inside:
             for nm, v in zip(names, r[5:9]):
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": sm[len(sm) // 2] if sm else None,
-                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
-                "reasons": sorted(reasons), "samples": len(rows)}
+                "sm_max_mhz": (float(inside[0][2]) if inside[0][2].replace(".", "").isdigit()
+                               else None),
+                "reasons": sorted(reasons), "samples_in_region": n_inside}
 
 
 def kernel_launches_per_step(plan, precision):
@@ -289,6 +319,7 @@ def run_ours(args):
         step()
     plan.sync_check()
     clocks.start()
+    clocks.mark()
     ms, bn = timed(step, args.steps, 0)
     clk = clocks.stop()
     plan.sync_check()
@@ -564,6 +595,16 @@ def run_serving(args, dev, precision="bf16x3", sweep=()):
         return reqs
 
     server = serving.make_server(max_batch=4, device=dev)
+    try:
+        return _serve_legs(args, server, serving, pool, sizes, w, box, sets, spec_of, stream,
+                           precision, sweep)
+    finally:
+        server.close()
+
+
+def _serve_legs(args, server, serving, pool, sizes, w, box, sets, spec_of, stream, precision,
+                sweep):
+    import numpy as np
     warm = [serving.Request(-1, pool[n][0], box, spec_of(n, kind),
                             second=pool[n][1] if cross else None, precision=precision)
             for n in sizes for kind in sets for cross in (False, True)]
@@ -585,7 +626,7 @@ def run_serving(args, dev, precision="bf16x3", sweep=()):
     stats = serve(stream(rng, args.serve_requests, args.serve_rate))
     stats.update({"rate_rps": args.serve_rate,
                   "mix": "N %s, weights %s, 30%% cross, all/equilateral/squeezed"
-                         % (sizes, [round(x, 3) for x in w]),
+                         % (sizes, [round(float(x), 3) for x in w]),
                   "prepare_s": prep_s, "precision": precision, "max_batch": 4,
                   "batching": "per shell set (N, box, shell list), bin sets mixed",
                   "resident_groups": len(server.groups)})
@@ -601,7 +642,7 @@ def run_serving(args, dev, precision="bf16x3", sweep=()):
               and c["p99_ms"] <= SERVE_P99_BOUND_MS and c["throughput_rps"] >= 0.9 * c["rate_rps"]]
         stats["sweep"] = {"requests_per_rate": args.serve_sweep_requests, "curve": curve,
                           "knee_rps": max(ok) if ok else None,
-                          "knee": "highest offered rate served at >= 90% of the rate with "
+                          "knee": "highest offered rate served at >= 90%% of the rate with "
                                   "p99 <= %.0f ms" % SERVE_P99_BOUND_MS}
     return stats
 

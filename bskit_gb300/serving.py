@@ -244,6 +244,17 @@ class Scheduler(object):
                 del self.pending[key]
         return now
 
+    def close(self):
+        """Wait for the batches in flight, then destroy every group (device memory, graphs)."""
+        while self.busy:
+            self.step()
+        for g in list(self.groups):
+            self.backend.destroy_group(g)
+        self.groups = []
+        self.used = 0
+        if hasattr(self.backend, "close"):
+            self.backend.close()
+
     def run(self, requests, realtime=True, poll_sleep=0.0):
         """Feed requests at their arrival times (seconds after start) and serve them all."""
         reqs = sorted(requests, key=lambda r: r.arrival)
@@ -360,8 +371,16 @@ class EngineBackend(object):
 
     def destroy_group(self, g):
         for inst in g.instances:
+            inst.graphs = {}
+            inst.out = {}
+            inst.dmesh = []
             inst.plan.close()
         g.instances = []
+
+    def close(self):
+        self.gridinfo.clear()
+        self.torch.cuda.synchronize(self.device)
+        self.torch.cuda.empty_cache()
 
     # -------------------------------------------------------------- grid info
     def _gridinfo(self, inst, job):

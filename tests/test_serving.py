@@ -130,6 +130,22 @@ def test_requests_never_exceed_budget_wait_instead():
     assert all(k == 1 for _, k in be.launched)
 
 
+def test_close_finishes_batches_in_flight_then_destroys_every_group():
+    be = FakeBackend()
+    sch = serving.Scheduler(be, mem_budget=10 ** 6, max_batch=2, max_groups=2, clock=FakeClock())
+    reqs = [_req(i, n, arrival=0.0) for i, n in enumerate((32, 32, 32, 64))]
+    for r in reqs:
+        sch.submit(r)
+    sch.step()  # dispatch: batches in flight, none polled to completion yet
+    assert sch.busy
+    sch.close()
+    assert not sch.busy and sch.groups == [] and sch.used == 0
+    assert sorted(be.destroyed) == sorted(n for n, _ in be.created)
+    # the batches in flight were retired with their results, not dropped
+    assert sum(k for _, k in be.launched) >= 2
+    assert sum(r.B is not None for r in reqs) == sum(k for _, k in be.launched)
+
+
 def test_bad_requests_rejected_at_submission():
     kf = 2 * np.pi / 100.0
     spec = dict(kmin=kf, kmax=4 * kf, dk=2 * kf)
