@@ -147,22 +147,155 @@ __global__ void __launch_bounds__(THREADS) contract_simt_kernel(
 // (two 16-byte loads of P and one of F3 per 32 FMAs).  Warps whose 32 columns lie past the
 // tile's nc skip their multiply-adds.  FP32 sums over the slice, FP64 atomics across slices.
 namespace f32 {
+// The plain-FP32 path: work item = (tile of 128 pair rows x nc <= 64 columns, 8192-point
+// slice), one block of 128 threads.  Per 32-point chunk the block forms the 128 x 32 pair
+// products once in shared memory and runs a register-tiled outer product
+// C[r][c] += P[r][x] F3[c][x]; each thread holds 8 rows x CB columns, CB = 4, 6 or 8 chosen
+// per tile (tile widths 32, 48, 64).  The operand loads of the outer product, not the
+// multiply-adds, bound this kernel: a warp's 128-bit shared-memory load costs four wavefronts
+// whatever its broadcast, so the 8 x 8 thread tile (16 values loaded per 64 multiply-adds)
+// is what raises the arithmetic per wavefront.  The next chunk's source and column rows are
+// copied global -> shared with cp.async into the other half of a double buffer while the
+// current chunk is computed.
 constexpr int KC = 32;
-constexpr int THREADS = 256;
+constexpr int THREADS = 128;
 constexpr int ROWS = 128, COLS = 64, SRC = 64;
 constexpr int APITCH = ROWS + 4;    // A[x][r]
 constexpr int BPITCH = COLS + 4;    // B[x][c]
 constexpr int SPITCH = KC + 1;      // S[row][x]
 constexpr int64_t SLICE = 8192;
+constexpr int STAGE = SRC * KC / THREADS;  // values per thread and array of one chunk (16)
+static_assert(COLS == SRC, "one staging pattern for sources and columns");
 
 struct Smem {
   float A[KC][APITCH];
-  float B[KC][BPITCH];
-  float S1[SRC][SPITCH];
-  float S2[SRC][SPITCH];
+  float B[2][KC][BPITCH];
+  float S1[2][SRC][SPITCH];
+  float S2[2][SRC][SPITCH];
 };
 
-__global__ void __launch_bounds__(THREADS, 2)
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool ok) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src),
+               "r"(ok ? 4 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// The outer product of one chunk: thread rows r0 .. r0 + 7, columns c0 .. c0 + CB - 1.
+template <int CB>
+__device__ __forceinline__ void fma_chunk(const float (&A)[KC][APITCH],
+                                          const float (&B)[KC][BPITCH], int r0, int c0,
+                                          float (&acc)[8][8]) {
+#pragma unroll 4
+  for (int k = 0; k < KC; ++k) {
+    const float4 a0 = *reinterpret_cast<const float4*>(&A[k][r0]);
+    const float4 a1 = *reinterpret_cast<const float4*>(&A[k][r0 + 4]);
+    const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+    float bv[8];
+    if (CB == 8) {
+      const float4 b0 = *reinterpret_cast<const float4*>(&B[k][c0]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&B[k][c0 + 4]);
+      bv[0] = b0.x; bv[1] = b0.y; bv[2] = b0.z; bv[3] = b0.w;
+      bv[4] = b1.x; bv[5] = b1.y; bv[6] = b1.z; bv[7] = b1.w;
+    } else if (CB == 6) {  // c0 = 6 m: 8-byte aligned
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const float2 b = *reinterpret_cast<const float2*>(&B[k][c0 + 2 * q]);
+        bv[2 * q] = b.x;
+        bv[2 * q + 1] = b.y;
+      }
+      bv[6] = bv[7] = 0.f;
+    } else {
+      const float4 b0 = *reinterpret_cast<const float4*>(&B[k][c0]);
+      bv[0] = b0.x; bv[1] = b0.y; bv[2] = b0.z; bv[3] = b0.w;
+      bv[4] = bv[5] = bv[6] = bv[7] = 0.f;
+    }
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+#pragma unroll
+      for (int q = 0; q < CB; ++q) acc[p][q] = fmaf(av[p], bv[q], acc[p][q]);
+  }
+}
+
+template <int CB>
+__device__ __forceinline__ void run_item(Smem& sm, const TileDesc& td, const int16_t* row_i,
+                                         const int16_t* row_j, const int32_t* map,
+                                         const float* f1, const float* f2, const float* f3,
+                                         int n_shells, int64_t K, int64_t x_begin, int64_t x_end,
+                                         bool one_src, double* out) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // outer-product block of this warp: rows [32 warp, +32), all 8 CB columns
+  const int r0 = 32 * warp + 8 * (lane >> 3);
+  const int c0 = CB * (lane & 7);
+  // pair-product formation: row tid, all points of the chunk
+  const int ri = row_i[td.row_off + tid], rj = row_j[td.row_off + tid];
+  const int pi = ri >= 0 ? ri - td.i0 : -1, pj = ri >= 0 ? rj - td.j0 : -1;
+  // staging: value k of a thread is row (tid >> 5) + 4 k, point tid & 31 of the chunk
+  const int sx = tid & 31, srow = tid >> 5;
+  auto stage = [&](int buf, int64_t x0) {
+    const bool xin = x0 + sx < x_end;
+#pragma unroll
+    for (int k = 0; k < STAGE; ++k) {
+      const int row = srow + 4 * k;
+      const int s1 = td.i0 + row, s2 = td.j0 + row, l = td.l0 + row;
+      const bool ok1 = row < td.ni && s1 < n_shells && xin;
+      cp_async4(&sm.S1[buf][row][sx], f1 + (ok1 ? (int64_t)s1 * K + x0 + sx : 0), ok1);
+      if (!one_src) {
+        const bool ok2 = row < td.nj && s2 < n_shells && xin;
+        cp_async4(&sm.S2[buf][row][sx], f2 + (ok2 ? (int64_t)s2 * K + x0 + sx : 0), ok2);
+      }
+      const bool okb = row < td.nc && l < n_shells && xin;
+      cp_async4(&sm.B[buf][sx][row], f3 + (okb ? (int64_t)l * K + x0 + sx : 0), okb);
+    }
+    cp_async_commit();
+  };
+  float acc[8][8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+  stage(0, x_begin);
+  int buf = 0;
+  for (int64_t x0 = x_begin; x0 < x_end; x0 += KC) {
+    if (x0 + KC < x_end) {
+      stage(buf ^ 1, x0 + KC);
+      cp_async_wait<1>();  // this chunk's copies are complete, the next chunk's in flight
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    {
+      const float(*S1)[SPITCH] = sm.S1[buf];
+      const float(*S2)[SPITCH] = one_src ? sm.S1[buf] : sm.S2[buf];
+#pragma unroll 8
+      for (int xx = 0; xx < KC; ++xx) sm.A[xx][tid] = pi >= 0 ? S1[pi][xx] * S2[pj][xx] : 0.f;
+    }
+    __syncthreads();
+    fma_chunk<CB>(sm.A, sm.B[buf], r0, c0, acc);
+    __syncthreads();  // A and this buffer are rewritten next
+    buf ^= 1;
+  }
+#pragma unroll
+  for (int p = 0; p < 8; ++p) {
+#pragma unroll
+    for (int q = 0; q < CB; ++q) {
+      const int c = c0 + q;
+      if (c < td.nc) {
+        const int t = __ldg(map + td.map_off + c * kTileRows + r0 + p);
+        if (t >= 0) atomicAdd(out + t, (double)acc[p][q]);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(THREADS, 3)
     contract_f32_kernel(const TileDesc* __restrict__ tiles, int n_tiles,
                         const int16_t* __restrict__ row_i, const int16_t* __restrict__ row_j,
                         const int32_t* __restrict__ map, const float* __restrict__ f1,
@@ -171,86 +304,19 @@ __global__ void __launch_bounds__(THREADS, 2)
                         int64_t n_slices, double* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char f32_smem[];
   Smem& sm = *reinterpret_cast<Smem*>(f32_smem);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // outer-product block of this warp: rows [32 wr, +32), columns [32 wc, +32)
-  const int wr = warp & 3, wc = warp >> 2;
-  const int r0 = 32 * wr + 8 * (lane >> 3);   // this thread's 8 rows
-  const int c0 = 32 * wc + 4 * (lane & 7);    // and 4 columns
-  // pair-product formation: row fr, points [16 fh, +16)
-  const int fr = tid & (ROWS - 1), fh = tid >> 7;
   const int64_t n_items = (int64_t)n_tiles * n_slices;
   for (int64_t item = blockIdx.x; item < n_items; item += gridDim.x) {
     const int64_t sl = item / n_tiles;
     const TileDesc td = tiles[item % n_tiles];
     const bool one_src = f1 == f2 && td.i0 == td.j0;
-    const int ri = row_i[td.row_off + fr], rj = row_j[td.row_off + fr];
-    const int pi = ri >= 0 ? ri - td.i0 : -1, pj = ri >= 0 ? rj - td.j0 : -1;
-    const bool busy = 32 * wc < td.nc;
     const int64_t x_begin = k_begin + sl * SLICE;
     const int64_t x_end = min(k_end, x_begin + SLICE);
-    float acc[8][4];
-#pragma unroll
-    for (int a = 0; a < 8; ++a)
-#pragma unroll
-      for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
-    for (int64_t x0 = x_begin; x0 < x_end; x0 += KC) {
-      const int x = (int)(tid & 31);
-      const bool xin = x0 + x < x_end;
-      // source rows and column rows of the chunk (lanes along points: coalesced)
-      for (int row = tid >> 5; row < SRC; row += THREADS / 32) {
-        const int s1 = td.i0 + row;
-        sm.S1[row][x] = (row < td.ni && s1 < n_shells && xin) ? __ldg(f1 + (int64_t)s1 * K + x0 + x)
-                                                               : 0.f;
-        if (!one_src) {
-          const int s2 = td.j0 + row;
-          sm.S2[row][x] = (row < td.nj && s2 < n_shells && xin)
-                              ? __ldg(f2 + (int64_t)s2 * K + x0 + x) : 0.f;
-        }
-      }
-      for (int c = tid >> 5; c < COLS; c += THREADS / 32) {
-        const int l = td.l0 + c;
-        sm.B[x][c] = (c < td.nc && l < n_shells && xin) ? __ldg(f3 + (int64_t)l * K + x0 + x)
-                                                        : 0.f;
-      }
-      __syncthreads();
-      {
-        const float(*S2)[SPITCH] = one_src ? sm.S1 : sm.S2;
-#pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          const int xx = 16 * fh + e;
-          sm.A[xx][fr] = pi >= 0 ? sm.S1[pi][xx] * S2[pj][xx] : 0.f;
-        }
-      }
-      __syncthreads();
-      if (busy) {
-#pragma unroll 8
-        for (int k = 0; k < KC; ++k) {
-          const float4 a0 = *reinterpret_cast<const float4*>(&sm.A[k][r0]);
-          const float4 a1 = *reinterpret_cast<const float4*>(&sm.A[k][r0 + 4]);
-          const float4 b = *reinterpret_cast<const float4*>(&sm.B[k][c0]);
-          const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-          const float bv[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-          for (int p = 0; p < 8; ++p)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(av[p], bv[q], acc[p][q]);
-        }
-      }
-      __syncthreads();
-    }
-    if (busy) {
-#pragma unroll
-      for (int p = 0; p < 8; ++p) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int c = c0 + q;
-          if (c < td.nc) {
-            const int t = __ldg(map + td.map_off + c * kTileRows + r0 + p);
-            if (t >= 0) atomicAdd(out + t, (double)acc[p][q]);
-          }
-        }
-      }
-    }
+    if (td.nc <= 32)
+      run_item<4>(sm, td, row_i, row_j, map, f1, f2, f3, n_shells, K, x_begin, x_end, one_src, out);
+    else if (td.nc <= 48)
+      run_item<6>(sm, td, row_i, row_j, map, f1, f2, f3, n_shells, K, x_begin, x_end, one_src, out);
+    else
+      run_item<8>(sm, td, row_i, row_j, map, f1, f2, f3, n_shells, K, x_begin, x_end, one_src, out);
   }
 }
 }  // namespace f32
