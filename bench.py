@@ -73,7 +73,7 @@ def parse():
                     help="Poisson arrival rate, req/s")
     ap.add_argument("--serve-small", action="store_true",
                     help="serving mix without N=512 (weights renormalised)")
-    ap.add_argument("--serve-sweep", default="20,40,80,160,320",
+    ap.add_argument("--serve-sweep", default="20,40,80,160,320,640",
                     help="offered rates of the bf16x3 p99-vs-rate sweep ('' = none)")
     ap.add_argument("--serve-sweep-requests", type=int, default=300)
     ap.add_argument("--serve-only", action="store_true", help="run only the serving leg")
@@ -624,17 +624,30 @@ def _serve_legs(args, server, serving, pool, sizes, w, box, sets, spec_of, strea
                             second=pool[n][1] if cross else None, precision=precision)
             for n in sizes for kind in sets for cross in (False, True)]
     t0 = time.perf_counter()
-    for n in sizes:  # ahead of the stream: groups, graphs and grid information
-        server.prepare([r for r in warm if r.nmesh == n], groups=1 if n >= 512 else 2)
+    for n in sorted(sizes, reverse=True):  # ahead of the stream, largest grid first
+        # every group the scheduler may admit for N <= 256 (small), one for 512^3 (~30 GB)
+        server.prepare([r for r in warm if r.nmesh == n], groups=1 if n >= 512 else None)
     server.run(warm, realtime=False)
     prep_s = time.perf_counter() - t0
 
     def serve(reqs):
         server.done = []
         cap0 = server.backend.captures_at_dispatch
+        by0 = dict(server.backend.captures_at_dispatch_by_n)
+        log0 = len(server.log)
         server.run(reqs, realtime=True)
         st = serving.latency_stats(reqs)
         st["graph_captures_at_dispatch"] = server.backend.captures_at_dispatch - cap0
+        st["graph_captures_at_dispatch_by_n"] = {
+            str(n): c - by0.get(n, 0) for n, c in server.backend.captures_at_dispatch_by_n.items()
+            if c - by0.get(n, 0)}
+        ev = {}
+        for e in server.log[log0:]:
+            if e[0] in ("admit", "evict"):
+                k = "%ss_by_n" % e[0]
+                ev.setdefault(k, {})
+                ev[k][str(e[1][0])] = ev[k].get(str(e[1][0]), 0) + 1
+        st.update(ev)
         return st
 
     rng = np.random.default_rng(2024)
@@ -644,7 +657,11 @@ def _serve_legs(args, server, serving, pool, sizes, w, box, sets, spec_of, strea
                          % (sizes, [round(float(x), 3) for x in w]),
                   "prepare_s": prep_s, "precision": precision, "max_batch": 4,
                   "batching": "per shell set (N, box, shell list), bin sets mixed",
-                  "resident_groups": len(server.groups)})
+                  "resident_groups": len(server.groups),
+                  "prepared_groups_by_n": {str(n): sum(1 for g in server.groups
+                                                       if g.shell_key[0] == n
+                                                       and getattr(g, "pinned", False))
+                                           for n in sizes}})
     if sweep:
         curve = []
         for rate in sweep:
@@ -915,7 +932,8 @@ def main():
     elif args.serve_only:
         import torch
         torch.cuda.set_device(0)
-        stats = run_serving(args, torch.device("cuda", 0))
+        sweep = [float(r) for r in args.serve_sweep.split(",") if r] if args.serve_sweep else []
+        stats = run_serving(args, torch.device("cuda", 0), sweep=sweep)
         print(json.dumps({"metric": "serve p50/p99 latency", "unit": "ms", "serving": stats}))
     else:
         run_ours(args)

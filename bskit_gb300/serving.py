@@ -10,7 +10,8 @@ types) and a precision.  The server
   computed once;
 * admits work by HBM footprint: a group of engine instances for a shell set is
   created only when its measured footprint fits in the budget (idle groups of
-  other shell sets are evicted, least recently used first);
+  other shell sets are evicted, least recently used first; groups admitted by
+  ``prepare`` only when the requesting shell set has no group at all);
 * batches requests of one shell set -- one N_grid, box and shell list -- whatever
   their bin sets (all / equilateral / squeezed / isosceles, auto or cross) and
   precisions: a batch of up to ``max_batch`` such requests runs on the instances
@@ -160,8 +161,10 @@ class Scheduler(object):
         want = self.max_groups if groups is None else int(groups)
         for key, js in per_shell.items():
             while sum(1 for g in self.groups if g.shell_key == key) < want:
-                if self._admit_group(js[0]) is None:
+                g = self._admit_group(js[0])
+                if g is None:
                     break
+                g.pinned = True  # prepared ahead: never evicted to make room for another group
             for g in self.groups:
                 if g.shell_key == key:
                     for j in js:
@@ -181,9 +184,13 @@ class Scheduler(object):
                 return g
         return None
 
-    def _evict_for(self, need):
-        """Destroy idle groups (least recently used first) until ``need`` bytes fit."""
-        idle = [g for g in self.groups if g not in self.busy]
+    def _evict_for(self, need, pinned_too=False):
+        """Destroy idle groups (least recently used first) until ``need`` bytes fit.  Groups
+        admitted by ``prepare`` are kept unless ``pinned_too``."""
+        idle = [g for g in self.groups if g not in self.busy
+                and (pinned_too or not getattr(g, "pinned", False))]
+        if self.used - sum(g.footprint for g in idle) + need > self.mem_budget:
+            return False  # would not fit even with all of them gone: destroy nothing
         idle.sort(key=lambda g: self.last_used.get(g, 0.0))
         while self.used + need > self.mem_budget and idle:
             g = idle.pop(0)
@@ -194,19 +201,27 @@ class Scheduler(object):
         return self.used + need <= self.mem_budget
 
     def _admit_group(self, job):
-        if sum(1 for g in self.groups if g.shell_key == job.shell_key) >= self.max_groups:
+        have = sum(1 for g in self.groups if g.shell_key == job.shell_key)
+        if have >= self.max_groups:
             return None
+        sizes = []
         size = self.max_batch
         while size >= 1:
-            need = self.backend.group_footprint(job, size)
-            if self.used + need <= self.mem_budget or self._evict_for(need):
-                g = self.backend.create_group(job, size)
-                g.footprint = need
-                self.groups.append(g)
-                self.used += need
-                self.log.append(("admit", job.shell_key[:2], size, need))
-                return g
+            sizes.append(size)
             size //= 2
+        # the largest group that fits, evicting only groups not admitted by ``prepare``; a
+        # shell set with no group at all may then take prepared groups' memory, one that has
+        # a group waits for it instead
+        for pinned_too in ((False, True) if have == 0 else (False,)):
+            for size in sizes:
+                need = self.backend.group_footprint(job, size)
+                if self.used + need <= self.mem_budget or self._evict_for(need, pinned_too):
+                    g = self.backend.create_group(job, size)
+                    g.footprint = need
+                    self.groups.append(g)
+                    self.used += need
+                    self.log.append(("admit", job.shell_key[:2], size, need))
+                    return g
         return None
 
     # -------------------------------------------------------------- main step
@@ -307,6 +322,7 @@ class EngineBackend(object):
         self.probe = {}         # shell_key -> measured footprint of one instance
         self.captures = 0       # graphs captured (prepare + dispatch)
         self.captures_at_dispatch = 0
+        self.captures_at_dispatch_by_n = {}
 
     # -------------------------------------------------------------- resources
     def _new_instance(self, job):
@@ -450,6 +466,8 @@ class EngineBackend(object):
             if self.use_graphs:
                 if job.bin_key not in inst.graphs:
                     self.captures_at_dispatch += 1
+                    n = job.req.nmesh
+                    self.captures_at_dispatch_by_n[n] = self.captures_at_dispatch_by_n.get(n, 0) + 1
                 # capture before this request's mesh is staged: the capture's warm-up run
                 # overwrites the instance's mesh buffers
                 graph = self._graph(inst, stream, job)

@@ -98,6 +98,39 @@ def test_prepare_admits_groups_and_captures_every_bin_set_ahead():
     assert len(be.created) == 4 and all(r.B is not None for r in reqs)
 
 
+def test_prepared_groups_are_kept_unless_a_shell_set_has_no_group():
+    be = FakeBackend()
+    # 32^3 groups of 2 cost 640, 64^3 ones 1280: the budget holds two 32^3 groups and one 64^3
+    sch = serving.Scheduler(be, mem_budget=2600, max_batch=2, max_groups=2, clock=FakeClock())
+    sch.prepare([_req(0, 32)])
+    sch.prepare([_req(1, 64)], groups=1)
+    assert sorted(be.created) == [(32, 2), (32, 2), (64, 2)] and sch.used == 2560
+    # more 64^3 work than its prepared group takes at once: no second 64^3 group evicts the
+    # prepared 32^3 groups; the requests wait for the prepared group
+    reqs = [_req(10 + i, 64) for i in range(6)]
+    sch.run(reqs, realtime=False)
+    assert all(r.B is not None for r in reqs)
+    assert be.destroyed == [] and len(be.created) == 3
+    # a shell set with no group at all may still take a prepared group's memory
+    r = _req(20, 128)
+    sch.run([r], realtime=False)
+    assert r.B is not None and be.created[-1] == (128, 2)
+    assert sorted(be.destroyed) == [32, 32, 64]
+
+
+def test_no_eviction_for_a_group_that_cannot_fit_and_smaller_groups_tried_first():
+    be = FakeBackend()
+    # a 64^3 group of 4 (2560) cannot fit a 2000 budget even in an empty server; a group of
+    # 2 (1280) fits beside the prepared 16^3 group of 4 (640): it is admitted, and the
+    # prepared group is not destroyed on the way by the attempt at 4
+    sch = serving.Scheduler(be, mem_budget=2000, max_batch=4, max_groups=1, clock=FakeClock())
+    sch.prepare([_req(0, 16)])
+    r = _req(1, 64)
+    sch.run([r], realtime=False)
+    assert r.B is not None
+    assert be.created == [(16, 4), (64, 2)] and be.destroyed == []
+
+
 def test_admission_by_footprint_and_eviction():
     be = FakeBackend()
     # room for one group of 2 instances of N=32 (640) but not two groups of N=32 and N=64
