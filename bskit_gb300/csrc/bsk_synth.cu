@@ -197,11 +197,13 @@ __device__ __forceinline__ void dft_radix(float2* v, const FftPlan& pl) {
   else dft_small<R>(v, pl);
 }
 
-// One Stockham pass of radix R over `lines` sequences of length n (src -> dst).
+// One Stockham pass of radix R over `lines` sequences of length n (src -> dst).  Input
+// positions zlo .. zhi are known to be zero: they are neither read nor need to be written
+// (the first pass of a pruned transform, whose inputs outside the kept frequencies are zero).
 template <int R>
 __device__ __forceinline__ void fft_pass(const float2* __restrict__ src, float2* __restrict__ dst,
                                          int lines, int n, int Ns, const float2* __restrict__ tw,
-                                         const FftPlan& pl) {
+                                         const FftPlan& pl, int zlo = 1 << 30, int zhi = -1) {
   const int m = n / R;
   const int step = n / (Ns * R);
   const int ls = line_stride(n);
@@ -213,7 +215,10 @@ __device__ __forceinline__ void fft_pass(const float2* __restrict__ src, float2*
     float2* o = dst + line * ls;
     float2 v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = in[j + r * m];
+    for (int r = 0; r < R; ++r) {
+      const int q = j + r * m;
+      v[r] = (q >= zlo && q <= zhi) ? make_float2(0.f, 0.f) : in[q];
+    }
     if (Ns > 1) {  // the first pass has k = 0: unit twiddles
 #pragma unroll
       for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * step]);
@@ -228,10 +233,12 @@ __device__ __forceinline__ void fft_pass(const float2* __restrict__ src, float2*
 // Compile-time length: the pass sequence unrolled, every divisor a constant.
 template <int N, int L, int P, int Ns>
 __device__ __forceinline__ void run_passes(float2*& src, float2*& dst,
-                                           const float2* __restrict__ tw, const FftPlan& pl) {
+                                           const float2* __restrict__ tw, const FftPlan& pl,
+                                           int zlo = 1 << 30, int zhi = -1) {
   if constexpr (P < plan_np(N)) {
     constexpr int R = plan_radix(N, P);
-    fft_pass<R>(src, dst, L, N, Ns, tw, pl);
+    if (P == 0) fft_pass<R>(src, dst, L, N, Ns, tw, pl, zlo, zhi);
+    else fft_pass<R>(src, dst, L, N, Ns, tw, pl);
     __syncthreads();
     float2* t2 = src;
     src = dst;
@@ -244,10 +251,12 @@ __device__ __forceinline__ void run_passes(float2*& src, float2*& dst,
 template <int N, int L, int P, int Ns>
 __device__ __forceinline__ void run_passes_but_last(float2*& src, float2*& dst,
                                                     const float2* __restrict__ tw,
-                                                    const FftPlan& pl) {
+                                                    const FftPlan& pl, int zlo = 1 << 30,
+                                                    int zhi = -1) {
   if constexpr (P + 1 < plan_np(N)) {
     constexpr int R = plan_radix(N, P);
-    fft_pass<R>(src, dst, L, N, Ns, tw, pl);
+    if (P == 0) fft_pass<R>(src, dst, L, N, Ns, tw, pl, zlo, zhi);
+    else fft_pass<R>(src, dst, L, N, Ns, tw, pl);
     __syncthreads();
     float2* t2 = src;
     src = dst;
@@ -261,26 +270,27 @@ __device__ __forceinline__ void run_passes_but_last(float2*& src, float2*& dst,
 // result.  NC = n at compile time, or 0.
 template <int NC, int L>
 __device__ float2* fft_lines(float2* a, float2* b, const FftPlan& pl,
-                             const float2* __restrict__ tw) {
+                             const float2* __restrict__ tw, int zlo = 1 << 30, int zhi = -1) {
   float2* src = a;
   float2* dst = b;
   if constexpr (NC != 0) {
-    run_passes<NC, L, 0, 1>(src, dst, tw, pl);
+    run_passes<NC, L, 0, 1>(src, dst, tw, pl, zlo, zhi);
   } else {
     const int n = pl.n;
     int Ns = 1;
     for (int p = 0; p < pl.np; ++p) {
       const int R = pl.radix[p];
+      const int zl = p == 0 ? zlo : 1 << 30, zh = p == 0 ? zhi : -1;
       switch (R) {
-        case 16: fft_pass<16>(src, dst, L, n, Ns, tw, pl); break;
-        case 24: fft_pass<24>(src, dst, L, n, Ns, tw, pl); break;
-        case 12: fft_pass<12>(src, dst, L, n, Ns, tw, pl); break;
-        case 6: fft_pass<6>(src, dst, L, n, Ns, tw, pl); break;
-        case 8: fft_pass<8>(src, dst, L, n, Ns, tw, pl); break;
-        case 4: fft_pass<4>(src, dst, L, n, Ns, tw, pl); break;
-        case 2: fft_pass<2>(src, dst, L, n, Ns, tw, pl); break;
-        case 3: fft_pass<3>(src, dst, L, n, Ns, tw, pl); break;
-        default: fft_pass<5>(src, dst, L, n, Ns, tw, pl); break;
+        case 16: fft_pass<16>(src, dst, L, n, Ns, tw, pl, zl, zh); break;
+        case 24: fft_pass<24>(src, dst, L, n, Ns, tw, pl, zl, zh); break;
+        case 12: fft_pass<12>(src, dst, L, n, Ns, tw, pl, zl, zh); break;
+        case 6: fft_pass<6>(src, dst, L, n, Ns, tw, pl, zl, zh); break;
+        case 8: fft_pass<8>(src, dst, L, n, Ns, tw, pl, zl, zh); break;
+        case 4: fft_pass<4>(src, dst, L, n, Ns, tw, pl, zl, zh); break;
+        case 2: fft_pass<2>(src, dst, L, n, Ns, tw, pl, zl, zh); break;
+        case 3: fft_pass<3>(src, dst, L, n, Ns, tw, pl, zl, zh); break;
+        default: fft_pass<5>(src, dst, L, n, Ns, tw, pl, zl, zh); break;
       }
       __syncthreads();
       float2* t2 = src;
@@ -341,20 +351,19 @@ __global__ void __launch_bounds__(kThreads) synth_x_kernel(SynthArgs A, FftPlan 
     sT[i] = code;
   }
   __syncthreads();
+  // positions R + 1 .. N - R - 1 of a line (|q_a| > R) are zero: not written, not read
+  const int zlo = nk == N ? 1 << 30 : A.R + 1, zhi = nk == N ? -1 : N - A.R - 1;
   for (int s = 0; s < A.ns; ++s) {
-    for (int i = threadIdx.x; i < kXLines * N; i += blockDim.x) {
-      const int a = i / kXLines, l = i - a * kXLines;
-      // position a of line l holds frequency index a
-      const int qa = fft_freq(a, N);
-      float2 v = make_float2(0.f, 0.f);
-      if (nk == N || (qa >= -A.R && qa <= A.R)) {
-        const int ak = nk == N ? a : qa + A.R;
-        if (in_shell(sT[ak * kXLines + l], A.s0 + s)) v = sS[ak * kXLines + l];
-      }
+    for (int i = threadIdx.x; i < kXLines * nk; i += blockDim.x) {
+      const int ak = i / kXLines, l = i - ak * kXLines;
+      // kept frequency ak sits at position a of line l (frequency index a)
+      const int a = kept_index(ak, nk, A.R, N);
+      const float2 v = in_shell(sT[ak * kXLines + l], A.s0 + s) ? sS[ak * kXLines + l]
+                                                                 : make_float2(0.f, 0.f);
       buf0[l * ls + a] = v;
     }
     __syncthreads();
-    const float2* res = fft_lines<NC, kXLines>(buf0, buf1, pl, tw);
+    const float2* res = fft_lines<NC, kXLines>(buf0, buf1, pl, tw, zlo, zhi);
     // G[s][x][bk][c0 + l]
     float2* g = A.G + (((int64_t)s * N) * nk + bk) * A.Cp + c0;
     for (int i = threadIdx.x; i < kXLines * N; i += blockDim.x) {
@@ -414,15 +423,11 @@ __global__ void __launch_bounds__(kThreads, 2) synth_y_kernel(SynthArgs A, FftPl
       const int bk = i / kLines, l = i - bk * kLines;
       buf0[l * ls + kept_index(bk, nk, A.R, N)] = g[(int64_t)bk * A.Cp + l];
     }
-    if (nk < N) {
-      for (int i = threadIdx.x; i < (N - nk) * kLines; i += kThreads) {
-        const int b = A.R + 1 + i / kLines, l = i % kLines;
-        buf0[l * ls + b] = make_float2(0.f, 0.f);
-      }
-    }
+    // positions R + 1 .. N - R - 1 (|q_b| > R) are zero: not written, not read
     __syncthreads();
     if (u + (int)gridDim.x < units) fetch(u + gridDim.x);
-    const float2* res = fft_lines<NC, kLines>(buf0, buf1, pl, tw);
+    const float2* res = nk < N ? fft_lines<NC, kLines>(buf0, buf1, pl, tw, A.R + 1, N - A.R - 1)
+                               : fft_lines<NC, kLines>(buf0, buf1, pl, tw);
     const int s = u / (N * nrun), r = u - s * (N * nrun);
     const int x = r / nrun, c0 = (r - x * nrun) * kLines;
     float2* h = A.Hh + (((int64_t)s * N + x) * N) * A.Cp + c0;
@@ -536,7 +541,7 @@ __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPl
         put(line, c, z1, z2);
       }
     }
-    for (int c = cn + cl; c <= N - cn; c += tpl) line[c] = make_float2(0.f, 0.f);
+    // positions cn .. N - cn (|q_c| >= cn) are zero: not written, not read
     __syncthreads();
     if (u + (int)gridDim.x < units) fetch(u + gridDim.x);
     const int64_t K = (int64_t)N * N * N;
@@ -545,10 +550,10 @@ __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPl
     if constexpr (NC != 0) {
       float2* src = buf0;
       float2* dst = buf1;
-      run_passes_but_last<NC, kZLines, 0, 1>(src, dst, tw, pl);
+      run_passes_but_last<NC, kZLines, 0, 1>(src, dst, tw, pl, cn, N - cn);
       z_last_pass<NC>(src, tw, pl, A, sh, row0, y0);
     } else {
-      const float2* res = fft_lines<NC, kZLines>(buf0, buf1, pl, tw);
+      const float2* res = fft_lines<NC, kZLines>(buf0, buf1, pl, tw, cn, N - cn);
       // four consecutive z per thread: 16-byte field stores, 8-byte hi / lo stores (N % 4 == 0)
       const int nq = N / 4;
       for (int i = threadIdx.x; i < 2 * kZLines * nq; i += kThreads) {
