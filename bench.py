@@ -232,14 +232,22 @@ class ClockSampler(object):
                 "reasons": sorted(reasons), "samples_in_region": n_inside}
 
 
-def kernel_launches_per_step(plan, precision):
-    """Kernels of libbskit_gb300 launched by one step (cuFFT's own kernels excluded)."""
-    chunks = (plan.n_shells + 7) // 8
-    n = 1 + chunks  # extract + filter chunks
-    if precision in ("bf16x3", "bf16"):
-        n += 1  # split
-    n += 1 + 1 + 1  # contraction + scale + normalize
-    return n
+def kernel_launches_per_step(plan, ts, slots=(0, 0, 0)):
+    """Kernels of libbskit_gb300 launched by one step (cuFFT's R2C kernels excluded): the
+    spectrum extraction of each painted slot; per grid level the level's spectrum (levels
+    below the plan's grid), the field synthesis (X, Y, Z passes per batch of 8 shells, the
+    bf16 split written by the Z pass) and one contraction; the normalisation."""
+    nslot = len(set(slots))
+    levels = ts.levels()
+    n = nslot
+    if levels:
+        for lv in levels:
+            if lv["ngrid"] != plan.ngrid:
+                n += nslot
+            n += 3 * ((lv["shells"] + 7) // 8) * nslot + 1
+    else:
+        n += 3 * ((plan.n_shells + 7) // 8) * nslot + 1 + 1  # synthesis, contraction, scale
+    return n + 1
 
 
 def run_ours(args):
@@ -388,7 +396,13 @@ def run_ours(args):
     c_ms, b_tc = timed(lambda: plan.measure_b(ts, precision=prec), reps, 1)
     c_ms /= reps
     ng = plan.ngrid
-    algo_flops = 2.0 * len(tri) * float(ng) ** 3
+    # the contraction's work: 2 flops per bin and point of the grid the bin is contracted on
+    # (grid levels: bins of small shells on smaller grids); the single reduced grid's work
+    # 2 T Ng^3 is reported beside it
+    levels = ts.levels()
+    single_flops = 2.0 * len(tri) * float(ng) ** 3
+    algo_flops = (sum(2.0 * lv["bins"] * float(lv["ngrid"]) ** 3 for lv in levels)
+                  if levels else single_flops)
     sched_cols = None
     peaks, peak_kind = measured_peaks()
     peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
@@ -397,12 +411,22 @@ def run_ours(args):
     # (bf16x3: hi x [Bhi; Blo] and lo x Bhi) multiply-adds
     tiles, sum_nc, pair_rows = ts.schedule()
     terms = 3 if prec == "bf16x3" else 1
-    issued_flops = 2.0 * 128 * terms * sum_nc * float(ng) ** 3
+    if levels:
+        issued_flops = sum(2.0 * 128 * terms * lv["sum_nc"] * float(lv["ngrid"]) ** 3
+                           for lv in levels)
+        tiles = sum(lv["tiles"] for lv in levels)
+        sum_nc = sum(lv["sum_nc"] for lv in levels)
+        pair_rows = sum(lv["pair_rows"] for lv in levels)
+        useful = algo_flops / (2.0 * 128 * sum(lv["sum_nc"] * float(lv["ngrid"]) ** 3
+                                               for lv in levels))
+    else:
+        issued_flops = 2.0 * 128 * terms * sum_nc * float(ng) ** 3
+        useful = len(tri) / (128.0 * sum_nc)
     issued = {"flops_per_launch": issued_flops,
               "tflops": issued_flops / (c_ms / 1e3) / 1e12,
               "frac": issued_flops / (c_ms / 1e3) / 1e12 / peak,
               "tiles": tiles, "sum_nc": sum_nc, "pair_rows": pair_rows,
-              "useful_fraction": len(tri) / (128.0 * sum_nc)}
+              "useful_fraction": useful}
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "contract_tc_traffic.json")) as f:
@@ -513,12 +537,14 @@ def run_ours(args):
                               "two device buffers)",
                 "result_matches_device_step": bool(torch.allclose(
                     host_check, bn.detach().cpu().double(), rtol=1e-9, atol=0))},
-        "gpu_launches": kernel_launches_per_step(plan, prec) * args.steps,
+        "gpu_launches": kernel_launches_per_step(plan, ts) * args.steps,
         "roofline": {"kernel": "contract_tc_kernel (tcgen05 bf16x3)", "bound": "tensor",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "%s bf16_tflops_sustained" % peak_kind,
                      "algorithmic_flops_per_launch": algo_flops,
+                     "single_grid_flops_per_launch": single_flops,
+                     "grid_levels": levels,
                      "launch_ms": c_ms,
                      "issued": issued},
         "cpu_baseline": cpu,

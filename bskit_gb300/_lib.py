@@ -27,6 +27,7 @@ PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "bf16x3": PREC_BF16X3, "bf16
 
 GRID_REDUCED = 0
 GRID_NATIVE = 1
+GRID_REDUCED_SINGLE = 2
 
 INFO_NMESH, INFO_NGRID, INFO_NSHELLS, INFO_QMAX, INFO_FOOTPRINT, INFO_CHUNK, INFO_DEVICE, \
     INFO_STREAM = range(8)
@@ -50,6 +51,7 @@ SIGNATURES = [
     ("bsk_paint", _INT, [_VP, _INT, _VP, _VP]),
     ("bsk_paint_cic", _INT, [_VP, _INT, _VP, _INT, _VP]),
     ("bsk_triset_schedule", _INT, [_VP, _VP]),
+    ("bsk_triset_levels", _INT, [_VP, _VP, _INT]),
     ("bsk_paint_subbox", _INT, [_VP, _INT, _VP, _INT, _INT, _INT, _INT, _VP]),
     ("bsk_compensate_cic", _INT, [_INT, _INT, _VP, _VP, _VP]),
     ("bsk_measure_b", _INT, [_VP, _VP, _INT, _INT, _INT, _INT, _VP, _VP]),

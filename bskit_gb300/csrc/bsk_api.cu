@@ -160,9 +160,9 @@ void bind_work(bsk_plan* p, cufftHandle h, cudaStream_t st) {
 }
 
 // Device bytes the plan holds: shell table, filter staging, per-slot spectra,
-// fields and bf16 splits, and the shared cuFFT work area.
-int64_t footprint(const bsk_plan* p) {
-  int64_t fp = (int64_t)p->Mh * 2 + (int64_t)p->chunk * p->Mh * 8;
+// fields and bf16 splits, and the shared cuFFT work area; with its grid-level plans.
+int64_t own_footprint(const bsk_plan* p) {
+  int64_t fp = (int64_t)p->Mh * 2 + (p->chunk_spec ? (int64_t)p->chunk * p->Mh * 8 : 0);
   for (const auto& s : p->slot) {
     if (s.spec) fp += p->Mh * 8;
     if (s.fields) fp += (int64_t)p->n_alloc() * p->K * 4;
@@ -173,14 +173,22 @@ int64_t footprint(const bsk_plan* p) {
   return fp + (int64_t)p->work_bytes;
 }
 
-// Refuse an allocation of `bytes` that would take the plan above its budget.
+int64_t footprint(const bsk_plan* p) {
+  int64_t fp = own_footprint(p);
+  for (const bsk_plan* q : p->levels) fp += own_footprint(q);
+  return fp;
+}
+
+// Refuse an allocation of `bytes` that would take the plan (with its grid levels: the
+// budget is the root plan's) above its budget.
 void check_budget(const bsk_plan* p, size_t bytes, const char* what) {
-  if (p->mem_budget == 0) return;
-  const int64_t after = footprint(p) + (int64_t)bytes;
-  if (after > (int64_t)p->mem_budget)
+  const bsk_plan* root = p->parent ? p->parent : p;
+  if (root->mem_budget == 0) return;
+  const int64_t after = footprint(root) + (int64_t)bytes;
+  if (after > (int64_t)root->mem_budget)
     throw Error{BSK_ERR_OOM, std::string(what) + " would take the plan to " +
                                  std::to_string(after) + " bytes, above its budget of " +
-                                 std::to_string(p->mem_budget)};
+                                 std::to_string(root->mem_budget)};
 }
 
 void release_stream(bsk_plan* p) {
@@ -205,13 +213,16 @@ void alloc_split(bsk_plan* p, FieldSlot& f) {
   BSK_CHECK_CUDA(cudaMemset(f.split, 0, bytes));
 }
 
-// Masked shell fields of `slot` for every shell.  With a grid the field synthesis
-// supports, its pruned FFT passes write the fields (and, when `with_split`, their bf16
-// hi / lo planes in the same pass); otherwise filter kernel + batched cuFFT C2R.
-void ensure_fields(bsk_plan* p, int s, cudaStream_t st, bool with_split = false) {
+// Masked shell fields of `slot` for shells [0, n_need) (every shell by default).  With a
+// grid the field synthesis supports, its pruned FFT passes write the fields (and, when
+// `with_split`, their bf16 hi / lo planes in the same pass) batch by batch; otherwise filter
+// kernel + batched cuFFT C2R for every shell.
+void ensure_fields(bsk_plan* p, int s, cudaStream_t st, bool with_split = false,
+                   int n_need = -1) {
   FieldSlot& f = p->slot[s];
   BSK_REQUIRE(f.painted, BSK_ERR_STATE, "field slot " + std::to_string(s) + " was not painted");
-  if (f.fields_ok) return;
+  const int need = n_need < 0 ? p->n : std::min(n_need, p->n);
+  if (f.fields_ok && f.fields_n >= need) return;
   if (!f.fields) {
     check_budget(p, (size_t)p->n_alloc() * p->K * sizeof(float), "the shell fields");
     f.fields = (float*)dmalloc((size_t)p->n_alloc() * p->K * sizeof(float));
@@ -226,14 +237,17 @@ void ensure_fields(bsk_plan* p, int s, cudaStream_t st, bool with_split = false)
       synth_init_workspace(p->Ng, p->synth_ws);
     }
     if (with_split) alloc_split(p, f);
-    for (int s0 = 0; s0 < p->n; s0 += p->chunk) {
+    int done = 0;
+    for (int s0 = 0; s0 < need; s0 += p->chunk) {
       const int ns = std::min(p->chunk, p->n - s0);
       int R = 0;
       for (int k = s0; k < s0 + ns; ++k) R = std::max(R, p->shell_r[k]);
       launch_synth(p->Ng, f.spec, p->table, s0, ns, R, p->synth_ws, f.fields,
                    with_split ? f.split : nullptr, p->n_alloc(), st);
+      done = s0 + ns;
     }
     f.fields_ok = true;
+    f.fields_n = done;
     f.split_ok = with_split;
     return;
   }
@@ -248,12 +262,13 @@ void ensure_fields(bsk_plan* p, int s, cudaStream_t st, bool with_split = false)
     BSK_CHECK_CUFFT(cufftExecC2R(p->c2r, p->chunk_spec, f.fields + (size_t)s0 * p->K));
   }
   f.fields_ok = true;
+  f.fields_n = p->n;
   f.split_ok = false;
 }
 
-void ensure_split(bsk_plan* p, int s, cudaStream_t st) {
+void ensure_split(bsk_plan* p, int s, cudaStream_t st, int n_need = -1) {
   FieldSlot& f = p->slot[s];
-  ensure_fields(p, s, st, true);
+  ensure_fields(p, s, st, true, n_need);
   if (f.split_ok) return;
   alloc_split(p, f);
   launch_split(f.fields, p->n_alloc(), p->K, f.split, st);
@@ -271,6 +286,7 @@ void destroy_triset(bsk_triset* set) {
   if (!set) return;
   DeviceGuard g(set->plan->device);
   set->sched.release();
+  for (auto& lv : set->levels) lv.sched.release();
   for (auto& kv : set->groups)
     for (auto& g : kv.second) g.sched.release();
   if (set->dups) cudaFree(set->dups);
@@ -281,6 +297,8 @@ void destroy_plan(bsk_plan* p) {
   if (!p) return;
   DeviceGuard g(p->device);
   cudaDeviceSynchronize();
+  for (bsk_plan* q : p->levels) destroy_plan(q);
+  p->levels.clear();
   for (auto& s : p->slot) free_slot(s);
   if (p->table) cudaFree(p->table);
   if (p->d_edges) cudaFree(p->d_edges);
@@ -500,6 +518,234 @@ void measure_b_stream(bsk_plan* p, const bsk_triset* set, int a, int b, int c, i
   p->last_stream_C = C;
 }
 
+// ---------------------------------------------------------------- grid levels
+// A bin (i, j, l) is exact on any grid of side Ng > r_i + r_j + r_l (the three wavevectors of
+// a closed triangle cannot wrap around), with each of its shells inside the grid's Nyquist
+// range (2 r < Ng); r_s is the largest |q_c| of a mode of shell s.  The plan's reduced grid
+// satisfies both for every bin; bins of small shells are contracted on smaller grids, at a
+// cost proportional to Ng^3 per point, with the shells they use synthesised on those grids.
+
+// The grid-level plan of side Ng holding shells [0, n) of p (one is made when none holds
+// enough shells).  Its spectra come from p's slots (launch_subgrid); it has no transforms of
+// its own besides the field synthesis.
+bsk_plan* level_plan(bsk_plan* p, int Ng, int n) {
+  for (bsk_plan* q : p->levels)
+    if (q->Ng == Ng && q->n >= n) return q;
+  std::unique_ptr<bsk_plan, void (*)(bsk_plan*)> q(new bsk_plan(), destroy_plan);
+  q->device = p->device;
+  q->num_sms = p->num_sms;
+  q->N = p->N;
+  q->L = p->L;
+  q->n = n;
+  q->parent = p;
+  q->edges.assign(p->edges.begin(), p->edges.begin() + 2 * n);
+  q->shell_r.assign(p->shell_r.begin(), p->shell_r.begin() + n);
+  q->qmax = 0;
+  for (int r : q->shell_r) q->qmax = std::max(q->qmax, r);
+  BSK_REQUIRE(2 * q->qmax < Ng, BSK_ERR_STATE, "internal: a level's shell exceeds its grid");
+  q->Ng = Ng;
+  q->K = (int64_t)Ng * Ng * Ng;
+  q->Mh = (int64_t)Ng * Ng * (Ng / 2 + 1);
+  q->chunk = std::min(n, 8);
+  check_budget(p, (size_t)q->Mh * sizeof(uint16_t), "a grid level's shell table");
+  q->table = (uint16_t*)dmalloc((size_t)q->Mh * sizeof(uint16_t));
+  q->d_edges = (double*)dmalloc((size_t)2 * n * sizeof(double));
+  BSK_CHECK_CUDA(cudaMemcpy(q->d_edges, q->edges.data(), 2 * n * sizeof(double),
+                            cudaMemcpyHostToDevice));
+  int hf[2] = {0, 0};
+  {
+    SyncTemp counts_t(n * sizeof(unsigned long long));
+    SyncTemp flag_t(2 * sizeof(int));
+    BSK_CHECK_CUDA(cudaMemset(counts_t.ptr, 0, n * sizeof(unsigned long long)));
+    BSK_CHECK_CUDA(cudaMemset(flag_t.ptr, 0, 2 * sizeof(int)));
+    launch_shell_table(q.get(), (unsigned long long*)counts_t.ptr, (int*)flag_t.ptr, 0);
+    BSK_CHECK_CUDA(cudaMemcpy(hf, flag_t.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+  }
+  BSK_REQUIRE(hf[0] == 0 && hf[1] <= q->qmax, BSK_ERR_STATE,
+              "internal: a grid level's shell table disagrees with its plan");
+  q->use_synth = synth_supported(Ng);
+  BSK_REQUIRE(q->use_synth, BSK_ERR_STATE, "internal: no field synthesis for a grid level");
+  q->synth_ws_bytes = synth_workspace_bytes(Ng, q->qmax, q->chunk);
+  p->levels.push_back(q.get());
+  return q.release();
+}
+
+// Slot s of a level plan from the parent's slot (again after every paint of the parent).
+void sync_level(bsk_plan* p, bsk_plan* q, int s, cudaStream_t st) {
+  const FieldSlot& pf = p->slot[s];
+  FieldSlot& qf = q->slot[s];
+  BSK_REQUIRE(pf.painted, BSK_ERR_STATE, "field slot " + std::to_string(s) + " was not painted");
+  if (qf.painted && qf.gen == pf.gen) return;
+  if (!qf.spec) {
+    check_budget(q, (size_t)q->Mh * sizeof(cufftComplex), "a grid level's spectrum");
+    qf.spec = (cufftComplex*)dmalloc((size_t)q->Mh * sizeof(cufftComplex));
+  }
+  launch_subgrid(p, q, pf.spec, qf.spec, st);
+  qf.painted = true;
+  qf.gen = pf.gen;
+  qf.fields_ok = false;
+  qf.split_ok = false;
+  qf.fields_n = 0;
+}
+
+// Grid sides the levels may take (below the plan's own): the sizes whose field synthesis is
+// compiled with constant strides.
+const int kLevelSides[] = {48, 96, 192, 256, 384, 480};
+// Per point: one 128-row tile of the tensor-core contraction costs ~13 field syntheses of a
+// shell (measured on the 384^3 grid: 2.44 ms per tile, 0.187 ms per shell of a batch of 8).
+constexpr double kTileCost = 13.0, kShellCost = 1.0;
+
+// Chooses the set's grid levels (minimum modelled cost over the subsets of the candidate
+// sides, the plan's own grid always last) and builds one schedule per level.
+void build_levels(bsk_plan* p, bsk_triset* set) {
+  std::vector<int> cand;
+  for (int n : kLevelSides)
+    if (n < p->Ng && synth_fast_size(n)) cand.push_back(n);
+  const int nt = (int)set->u_tri.size();
+  std::vector<int> need(nt), rmax(nt);
+  for (int t = 0; t < nt; ++t) {
+    const HostTriangle& h = set->u_tri[t];
+    const int ri = p->shell_r[h.i], rj = p->shell_r[h.j], rl = p->shell_r[h.l];
+    need[t] = ri + rj + rl;
+    rmax[t] = std::max(ri, std::max(rj, rl));
+  }
+  auto assign = [&](const std::vector<int>& sides, std::vector<int>& lev) {
+    lev.assign(nt, (int)sides.size() - 1);
+    for (int t = 0; t < nt; ++t)
+      for (int k = 0; k + 1 < (int)sides.size(); ++k)
+        if (need[t] < sides[k] && 2 * rmax[t] < sides[k]) {
+          lev[t] = k;
+          break;
+        }
+  };
+  double best = -1.0;
+  std::vector<int> best_sides;
+  const int nc = (int)cand.size();
+  for (int mask = 0; mask < (1 << nc); ++mask) {
+    std::vector<int> sides;
+    for (int k = 0; k < nc; ++k)
+      if (mask >> k & 1) sides.push_back(cand[k]);
+    sides.push_back(p->Ng);
+    std::vector<int> lev;
+    assign(sides, lev);
+    double cost = 0.0;
+    for (int k = 0; k < (int)sides.size(); ++k) {
+      std::vector<HostTriangle> tk;
+      int top = -1;
+      for (int t = 0; t < nt; ++t)
+        if (lev[t] == k) {
+          tk.push_back(set->u_tri[t]);
+          top = std::max(top, std::max(set->u_tri[t].i, std::max(set->u_tri[t].j,
+                                                                  set->u_tri[t].l)));
+        }
+      if (tk.empty()) continue;
+      HostSchedule hs;
+      tile_schedule(tk, p->n, nullptr, hs);
+      // every level synthesises the prefix of shells its bins use
+      const double k3 = std::pow((double)sides[k], 3);
+      cost += k3 * (kTileCost * hs.tiles.size() + kShellCost * (top + 1));
+    }
+    if (best < 0 || cost < best) {
+      best = cost;
+      best_sides = sides;
+    }
+  }
+  std::vector<int> lev;
+  assign(best_sides, lev);
+  for (int k = 0; k < (int)best_sides.size(); ++k) {
+    std::vector<HostTriangle> tk;
+    std::vector<int> idx;
+    int top = -1;
+    for (int t = 0; t < nt; ++t)
+      if (lev[t] == k) {
+        tk.push_back(set->u_tri[t]);
+        idx.push_back(set->u_idx[t]);
+        top = std::max(top, std::max(set->u_tri[t].i, std::max(set->u_tri[t].j,
+                                                                set->u_tri[t].l)));
+      }
+    if (tk.empty()) continue;
+    GridLevel lv;
+    lv.n_shells = top + 1;
+    lv.bins = (int64_t)tk.size();
+    lv.plan = k + 1 == (int)best_sides.size() ? p : level_plan(p, best_sides[k], top + 1);
+    set->levels.push_back(lv);
+    build_schedule(tk, lv.plan->n, set->levels.back().sched, &idx);
+  }
+}
+
+// A point range [k0, k1) of the plan's grid as the matching share of a level's grid
+// (128-point aligned, so that the ranges of consecutive shards tile the level's grid).
+int64_t level_point(int64_t k, int64_t K, int64_t Kq) {
+  if (k >= K) return Kq;
+  return (int64_t)((__int128)k * Kq / K) / 128 * 128;
+}
+
+// The resident path over the set's grid levels: every level adds its bins' scaled sums
+// into `out`.
+void measure_levels(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int precision,
+                    int64_t k0, int64_t k1, double* out, cudaStream_t st) {
+  const bool tc = precision == BSK_PREC_BF16X3 || precision == BSK_PREC_BF16;
+  BSK_CHECK_CUDA(cudaMemsetAsync(out, 0, (size_t)set->T * sizeof(double), st));
+  for (const GridLevel& lv : set->levels) {
+    bsk_plan* q = lv.plan;
+    const int nn = lv.n_shells;
+    if (q != p) {
+      sync_level(p, q, a, st);
+      if (b != a) sync_level(p, q, b, st);
+      if (c != a && c != b) sync_level(p, q, c, st);
+    }
+    if (tc) ensure_split(q, c, st, nn);  // first: a synthesis pass writes the split too
+    ensure_fields(q, a, st, false, nn);
+    ensure_fields(q, b, st, false, nn);
+    ensure_fields(q, c, st, false, nn);
+    if (tc) ensure_split(q, c, st, nn);
+    const int64_t q0 = level_point(k0, p->K, q->K), q1 = level_point(k1, p->K, q->K);
+    if (q1 <= q0) continue;
+    const double scale = std::pow(p->L, 6) / (double)q->K;
+    const float *fa = q->slot[a].fields, *fb = q->slot[b].fields, *fc = q->slot[c].fields;
+    switch (precision) {
+      case BSK_PREC_FP64:
+        launch_contract_simt_f64(lv.sched, fa, fb, fc, q->n, q->K, q0, q1, out, q->num_sms, st,
+                                 scale);
+        break;
+      case BSK_PREC_FP32:
+        launch_contract_simt_f32(lv.sched, fa, fb, fc, q->n, q->K, q0, q1, out, q->num_sms, st,
+                                 scale);
+        break;
+      default:
+        launch_contract_tc(lv.sched, fa, fb, q->slot[c].split, q->n_alloc(), q->n, q->K, q0,
+                           q1, precision == BSK_PREC_BF16X3 ? 3 : 1, out, q->num_sms, st,
+                           scale);
+        break;
+    }
+  }
+  copy_dups(set, out, st);
+}
+
+// Device bytes the resident path still has to allocate for slots a, b, c (and the split of
+// c) on every grid it uses.
+int64_t resident_need(const bsk_plan* p, const bsk_triset* set, int a, int b, int c, bool tc) {
+  std::vector<const bsk_plan*> grids;
+  if (set->levels.empty()) grids.push_back(p);
+  for (const GridLevel& lv : set->levels)
+    if (std::find(grids.begin(), grids.end(), lv.plan) == grids.end()) grids.push_back(lv.plan);
+  int64_t need = 0;
+  for (const bsk_plan* q : grids) {
+    bool seen[3] = {false, false, false};
+    for (int sl : {a, b, c})
+      if (!seen[sl]) {
+        seen[sl] = true;
+        if (!q->slot[sl].fields) need += (int64_t)q->n_alloc() * q->K * sizeof(float);
+        if (q != p && !q->slot[sl].spec) need += q->Mh * (int64_t)sizeof(cufftComplex);
+      }
+    if (tc && !q->slot[c].split)
+      need += (int64_t)split_elems(q->n_alloc(), q->K) * sizeof(__nv_bfloat16);
+    // the field synthesis' workspace is allocated with the first resident fields
+    if (q->use_synth && !q->synth_ws) need += (int64_t)q->synth_ws_bytes;
+  }
+  return need;
+}
+
 void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int precision,
                int64_t k0, int64_t k1, double* out, cudaStream_t st) {
   BSK_REQUIRE(p && set, BSK_ERR_ARG, "NULL argument");
@@ -521,21 +767,12 @@ void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int prec
     return;
   }
   if (p->mem_budget) {
-    // resident path: all shells of each slot (and the split of the third) stay on the device
-    const size_t field_bytes = (size_t)p->n_alloc() * p->K * sizeof(float);
-    size_t need = 0;
-    bool seen[3] = {false, false, false};
-    for (int sl : {a, b, c})
-      if (!seen[sl]) {
-        seen[sl] = true;
-        if (!p->slot[sl].fields) need += field_bytes;
-      }
-    if (tc && !p->slot[c].split) need += split_elems(p->n_alloc(), p->K) * sizeof(__nv_bfloat16);
-    // the field synthesis' workspace is allocated with the first resident fields
-    if (p->use_synth && !p->synth_ws) need += p->synth_ws_bytes;
+    // resident path: all shells of each slot (and the split of the third) stay on the device,
+    // on every grid level of the set
+    const int64_t need = resident_need(p, set, a, b, c, tc);
     const int64_t held =
         p->stream_C ? (int64_t)p->stream_C * p->K * (12 + (p->stream_tc ? 4 : 0)) : 0;
-    if (footprint(p) - held + (int64_t)need > (int64_t)p->mem_budget) {
+    if (footprint(p) - held + need > (int64_t)p->mem_budget) {
       measure_b_stream(p, set, a, b, c, precision, k0, k1, out, st);
       launch_scale(out, set->T, std::pow(p->L, 6) / (double)p->K, st);
       return;
@@ -543,6 +780,10 @@ void measure_b(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int prec
     release_stream(p);
   }
   p->last_stream_C = 0;
+  if (!set->levels.empty()) {
+    measure_levels(p, set, a, b, c, precision, k0, k1, out, st);
+    return;
+  }
   if (tc) ensure_split(p, c, st);  // first, so that a synthesis pass writes the split as well
   ensure_fields(p, a, st);
   ensure_fields(p, b, st);
@@ -679,8 +920,9 @@ int bsk_plan_create(int nmesh, double box_size, int n_shells, const double* shel
     BSK_REQUIRE(std::isfinite(box_size) && box_size > 0, BSK_ERR_ARG, "BoxSize must be > 0");
     BSK_REQUIRE(n_shells >= 1 && n_shells <= 255, BSK_ERR_ARG, "need 1..255 shells");
     BSK_REQUIRE(shell_edges, BSK_ERR_ARG, "shell_edges is NULL");
-    BSK_REQUIRE(grid_mode == BSK_GRID_REDUCED || grid_mode == BSK_GRID_NATIVE, BSK_ERR_ARG,
-                "bad grid mode");
+    BSK_REQUIRE(grid_mode == BSK_GRID_REDUCED || grid_mode == BSK_GRID_NATIVE ||
+                    grid_mode == BSK_GRID_REDUCED_SINGLE,
+                BSK_ERR_ARG, "bad grid mode");
     // an error before the plan is handed out releases what it holds so far
     std::unique_ptr<bsk_plan, void (*)(bsk_plan*)> p(new bsk_plan(), destroy_plan);
     BSK_CHECK_CUDA(cudaGetDevice(&p->device));
@@ -739,6 +981,7 @@ int bsk_plan_create(int nmesh, double box_size, int n_shells, const double* shel
     }
     p->use_synth = synth_supported(p->Ng);
     if (p->use_synth) p->synth_ws_bytes = synth_workspace_bytes(p->Ng, qmax, p->chunk);
+    p->use_levels = grid_mode == BSK_GRID_REDUCED && p->Ng != p->N && p->use_synth;
     make_r2c(p.get());
     make_c2r(p.get());
     p->chunk_spec = (cufftComplex*)dmalloc((size_t)p->chunk * p->Mh * sizeof(cufftComplex));
@@ -811,6 +1054,7 @@ int bsk_triset_create(bsk_plan* p, int64_t n_tri, const int32_t* tri, bsk_triset
         }
     }
     build_schedule(s->u_tri, p->n, s->sched, &s->u_idx);
+    if (p->use_levels && !s->u_tri.empty()) build_levels(p, s.get());
     if (!dups.empty()) {
       s->n_dups = (int)dups.size();
       s->dups = (int2*)dmalloc(dups.size() * sizeof(int2));
@@ -819,6 +1063,30 @@ int bsk_triset_create(bsk_plan* p, int64_t n_tri, const int32_t* tri, bsk_triset
     }
     *out = s.release();
   });
+}
+
+int bsk_triset_levels(const bsk_triset* set, int64_t* out, int cap) {
+  int n = -1;
+  const int rc = guarded([&] {
+    BSK_REQUIRE(set && (cap == 0 || out), BSK_ERR_ARG, "NULL argument");
+    n = (int)set->levels.size();
+    for (int k = 0; k < n && k < cap; ++k) {
+      const GridLevel& lv = set->levels[k];
+      int64_t cols = 0, rows = 0;
+      for (const TileDesc& d : lv.sched.h_tiles) {
+        cols += d.nc;
+        rows += d.nrows;
+      }
+      int64_t* o = out + 6 * k;
+      o[0] = lv.plan->Ng;
+      o[1] = lv.sched.n_tiles;
+      o[2] = cols;
+      o[3] = rows;
+      o[4] = lv.bins;
+      o[5] = lv.n_shells;
+    }
+  });
+  return rc == BSK_OK ? n : rc;
 }
 
 int bsk_triset_destroy(bsk_triset* set) {

@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(THREADS) contract_simt_kernel(
     const int16_t* __restrict__ row_i, const int16_t* __restrict__ row_j,
     const int32_t* __restrict__ map, const Tin* __restrict__ f1, const Tin* __restrict__ f2,
     const Tin* __restrict__ f3, int n_shells, int64_t K, int64_t k_begin, int64_t k_end,
-    int64_t slice, int64_t n_slices, double* __restrict__ out) {
+    int64_t slice, int64_t n_slices, double* __restrict__ out, double scale) {
   extern __shared__ __align__(16) unsigned char simt_smem[];
   typedef Tacc ATile[KC][ROWS + APAD];
   typedef Tacc BTile[KC][COLS + BPAD];
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(THREADS) contract_simt_kernel(
         const int c = c0 + tx * 4 + q;
         if (c < td.nc) {
           const int t = map[td.map_off + c * ROWS + r];
-          if (t >= 0) atomicAdd(out + t, (double)acc[p][q]);
+          if (t >= 0) atomicAdd(out + t, (double)acc[p][q] * scale);
         }
       }
     }
@@ -229,7 +229,7 @@ __device__ __forceinline__ void run_item(Smem& sm, const TileDesc& td, const int
                                          const int16_t* row_j, const int32_t* map,
                                          const float* f1, const float* f2, const float* f3,
                                          int n_shells, int64_t K, int64_t x_begin, int64_t x_end,
-                                         bool one_src, double* out) {
+                                         bool one_src, double* out, double scale) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // outer-product block of this warp: rows [32 warp, +32), all 8 CB columns
   const int r0 = 32 * warp + 8 * (lane >> 3);
@@ -289,7 +289,7 @@ __device__ __forceinline__ void run_item(Smem& sm, const TileDesc& td, const int
       const int c = c0 + q;
       if (c < td.nc) {
         const int t = __ldg(map + td.map_off + c * kTileRows + r0 + p);
-        if (t >= 0) atomicAdd(out + t, (double)acc[p][q]);
+        if (t >= 0) atomicAdd(out + t, (double)acc[p][q] * scale);
       }
     }
   }
@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(THREADS, 3)
                         const int32_t* __restrict__ map, const float* __restrict__ f1,
                         const float* __restrict__ f2, const float* __restrict__ f3,
                         int n_shells, int64_t K, int64_t k_begin, int64_t k_end,
-                        int64_t n_slices, double* __restrict__ out) {
+                        int64_t n_slices, double* __restrict__ out, double scale) {
   extern __shared__ __align__(16) unsigned char f32_smem[];
   Smem& sm = *reinterpret_cast<Smem*>(f32_smem);
   const int64_t n_items = (int64_t)n_tiles * n_slices;
@@ -312,11 +312,11 @@ __global__ void __launch_bounds__(THREADS, 3)
     const int64_t x_begin = k_begin + sl * SLICE;
     const int64_t x_end = min(k_end, x_begin + SLICE);
     if (td.nc <= 32)
-      run_item<4>(sm, td, row_i, row_j, map, f1, f2, f3, n_shells, K, x_begin, x_end, one_src, out);
+      run_item<4>(sm, td, row_i, row_j, map, f1, f2, f3, n_shells, K, x_begin, x_end, one_src, out, scale);
     else if (td.nc <= 48)
-      run_item<6>(sm, td, row_i, row_j, map, f1, f2, f3, n_shells, K, x_begin, x_end, one_src, out);
+      run_item<6>(sm, td, row_i, row_j, map, f1, f2, f3, n_shells, K, x_begin, x_end, one_src, out, scale);
     else
-      run_item<8>(sm, td, row_i, row_j, map, f1, f2, f3, n_shells, K, x_begin, x_end, one_src, out);
+      run_item<8>(sm, td, row_i, row_j, map, f1, f2, f3, n_shells, K, x_begin, x_end, one_src, out, scale);
   }
 }
 }  // namespace f32
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(THREADS, 3)
 template <typename Tin, typename Tacc>
 void launch_simt(const DeviceSchedule& s, const Tin* f1, const Tin* f2, const Tin* f3,
                  int n_shells, int64_t K, int64_t k_begin, int64_t k_end, int64_t slice,
-                 double* out, int num_sms, cudaStream_t st) {
+                 double* out, int num_sms, cudaStream_t st, double scale) {
   if (s.n_sub == 0 || k_end <= k_begin) return;
   const size_t smem = 2 * sizeof(Tacc) * KC * ((ROWS + APAD) + (COLS + BPAD));
   BSK_CHECK_CUDA(cudaFuncSetAttribute(contract_simt_kernel<Tin, Tacc>,
@@ -339,7 +339,7 @@ void launch_simt(const DeviceSchedule& s, const Tin* f1, const Tin* f2, const Ti
   if (grid > n_items) grid = n_items;
   contract_simt_kernel<Tin, Tacc><<<(unsigned)grid, THREADS, smem, st>>>(
       s.tiles, s.subs, s.n_sub, s.row_i, s.row_j, s.map, f1, f2, f3, n_shells, K, k_begin, k_end,
-      slice, n_slices, out);
+      slice, n_slices, out, scale);
   BSK_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -348,7 +348,8 @@ void launch_simt(const DeviceSchedule& s, const Tin* f1, const Tin* f2, const Ti
 // FP32 products and tile sums (8192-point slices), FP64 cross-slice sum.
 void launch_contract_simt_f32(const DeviceSchedule& s, const float* f1, const float* f2,
                               const float* f3, int n_shells, int64_t K, int64_t k_begin,
-                              int64_t k_end, double* out, int num_sms, cudaStream_t st) {
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st,
+                              double scale) {
   if (s.n_tiles == 0 || k_end <= k_begin) return;
   const size_t smem = sizeof(f32::Smem);
   BSK_CHECK_CUDA(cudaFuncSetAttribute(f32::contract_f32_kernel,
@@ -363,22 +364,26 @@ void launch_contract_simt_f32(const DeviceSchedule& s, const float* f1, const fl
   if (grid > n_items) grid = n_items;
   f32::contract_f32_kernel<<<(unsigned)grid, f32::THREADS, smem, st>>>(
       s.tiles, s.n_tiles, s.row_i, s.row_j, s.map, f1, f2, f3, n_shells, K, k_begin, k_end,
-      n_slices, out);
+      n_slices, out, scale);
   BSK_CHECK_CUDA(cudaGetLastError());
 }
 
 // FP64 products and sums of FP32 fields (the GPU oracle of the precision study).
 void launch_contract_simt_f64(const DeviceSchedule& s, const float* f1, const float* f2,
                               const float* f3, int n_shells, int64_t K, int64_t k_begin,
-                              int64_t k_end, double* out, int num_sms, cudaStream_t st) {
-  launch_simt<float, double>(s, f1, f2, f3, n_shells, K, k_begin, k_end, 65536, out, num_sms, st);
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st,
+                              double scale) {
+  launch_simt<float, double>(s, f1, f2, f3, n_shells, K, k_begin, k_end, 65536, out, num_sms, st,
+                             scale);
 }
 
 // FP64 fields (grid information).
 void launch_contract_simt_d64(const DeviceSchedule& s, const double* f1, const double* f2,
                               const double* f3, int n_shells, int64_t K, int64_t k_begin,
-                              int64_t k_end, double* out, int num_sms, cudaStream_t st) {
-  launch_simt<double, double>(s, f1, f2, f3, n_shells, K, k_begin, k_end, 65536, out, num_sms, st);
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st,
+                              double scale) {
+  launch_simt<double, double>(s, f1, f2, f3, n_shells, K, k_begin, k_end, 65536, out, num_sms, st,
+                              scale);
 }
 
 }  // namespace bsk

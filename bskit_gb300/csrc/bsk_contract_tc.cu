@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                        const int16_t* __restrict__ row_i, const int16_t* __restrict__ row_j,
                        const int32_t* __restrict__ map, int n_tiles, int same_src,
                        int64_t k_begin, int64_t k_end, int64_t n_items, int terms, int fused,
-                       double* __restrict__ out) {
+                       double* __restrict__ out, double scale) {
   constexpr int64_t slice = kLongSlice ? kSliceLong : kSliceShort;
   constexpr int STAGE_BYTES = Ring<kTwoSrc>::kStageBytes;
   constexpr int SST = Ring<kTwoSrc>::kStages;
@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int c = 0; c < 32; ++c) {
         if (c0 + c < td.nc) {
           const int t = __ldg(mp + c * kTileRows);
-          if (t >= 0) atomicAdd(out + t, (double)acc[c]);
+          if (t >= 0) atomicAdd(out + t, (double)acc[c] * scale);
         }
       }
     }
@@ -727,7 +727,7 @@ void make_split_map(CUtensorMap* m, const __nv_bfloat16* split, int S, int64_t K
 void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f2,
                         const __nv_bfloat16* f3_split, int split_shells, int n_shells,
                         int64_t K, int64_t k_begin, int64_t k_end, int terms, double* out,
-                        int num_sms, cudaStream_t st) {
+                        int num_sms, cudaStream_t st, double scale) {
   if (s.n_tiles == 0 || k_end <= k_begin) return;
   BSK_REQUIRE(k_begin % tc::KCH == 0, BSK_ERR_ARG, "k_begin must be a multiple of 128");
   BSK_REQUIRE(k_end % tc::KCH == 0 || k_end == K, BSK_ERR_ARG,
@@ -776,7 +776,7 @@ void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f
   if (grid > n_items) grid = n_items;
   kern<<<(unsigned)grid, tc::THREADS, smem, st>>>(
       m, s.tiles, s.row_i, s.row_j, s.map, s.n_tiles, f1 == f2 ? 1 : 0, k_begin, k_end,
-      n_items, terms, fused ? 1 : 0, out);
+      n_items, terms, fused ? 1 : 0, out, scale);
   BSK_CHECK_CUDA(cudaGetLastError());
 }
 

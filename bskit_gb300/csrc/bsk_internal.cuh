@@ -11,6 +11,8 @@
 
 #include "../../include/bskit_gb300.h"
 
+struct bsk_plan;
+
 namespace bsk {
 
 // ---------------------------------------------------------------- errors
@@ -128,7 +130,19 @@ struct FieldSlot {
   __nv_bfloat16* split = nullptr; // bf16 split of the n_alloc shells, chunk-major (above)
   bool fields_ok = false;
   bool split_ok = false;
-  int64_t gen = 0;                // bumped by every paint (keys of streamed fields)
+  int fields_n = 0;               // shells [0, fields_n) of `fields` (and `split`) are valid
+  int64_t gen = 0;                // bumped by every paint (keys of streamed fields); on a grid
+                                  // level's plan: the parent paint its spectrum was taken from
+};
+
+// One contraction grid of a triangle set: the bins whose three shells sum to less than the
+// grid side are contracted on it (exact: q1 + q2 + q3 cannot wrap around), with the shell
+// fields of the grid's plan (the set's own plan, or one of its grid-level plans).
+struct GridLevel {
+  bsk_plan* plan = nullptr;
+  DeviceSchedule sched;   // map entries are positions in the set's output
+  int n_shells = 0;       // shells [0, n_shells) the level's bins use
+  int64_t bins = 0;
 };
 
 }  // namespace bsk
@@ -174,6 +188,12 @@ struct bsk_plan {
   std::vector<int> shell_r;             // largest |q_c| of a mode in each shell
   void* synth_ws = nullptr;             // twiddles + X / Y pass intermediates of one batch
   size_t synth_ws_bytes = 0;
+  // grid levels: smaller contraction grids for bins of small shells (owned by the plan);
+  // a level's plan has `parent` set, takes its spectra from the parent's slots and holds a
+  // prefix of the parent's shells
+  bool use_levels = false;
+  bsk_plan* parent = nullptr;
+  std::vector<bsk_plan*> levels;
   int n_alloc() const { return (n + chunk - 1) / chunk * chunk; }  // shells rounded to batches
 };
 
@@ -188,6 +208,7 @@ struct bsk_triset {
   std::vector<bsk::HostTriangle> u_tri;  // first occurrences, in order
   std::vector<int> u_idx;                // their positions in the list
   mutable std::map<int, std::vector<bsk::StreamGroup>> groups;  // per streaming chunk size
+  std::vector<bsk::GridLevel> levels;    // the resident path's grids (empty: the plan's only)
 };
 
 namespace bsk {
@@ -225,22 +246,25 @@ void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0
 void launch_split(const float* in, int S, int64_t K, __nv_bfloat16* split, cudaStream_t st);
 
 // SIMT contraction (Tin = float|double input fields, Tacc = float|double tile sums).
-// out[t] += sum over K of f1[i] f2[j] f3[l]  (out must be zeroed by the caller).
+// out[t] += scale * sum over K of f1[i] f2[j] f3[l]  (out must be zeroed by the caller).
 void launch_contract_simt_f32(const DeviceSchedule& s, const float* f1, const float* f2,
                               const float* f3, int n_shells, int64_t K, int64_t k_begin,
-                              int64_t k_end, double* out, int num_sms, cudaStream_t st);
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st,
+                              double scale = 1.0);
 void launch_contract_simt_f64(const DeviceSchedule& s, const float* f1, const float* f2,
                               const float* f3, int n_shells, int64_t K, int64_t k_begin,
-                              int64_t k_end, double* out, int num_sms, cudaStream_t st);
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st,
+                              double scale = 1.0);
 void launch_contract_simt_d64(const DeviceSchedule& s, const double* f1, const double* f2,
                               const double* f3, int n_shells, int64_t K, int64_t k_begin,
-                              int64_t k_end, double* out, int num_sms, cudaStream_t st);
+                              int64_t k_end, double* out, int num_sms, cudaStream_t st,
+                              double scale = 1.0);
 
 // tcgen05 contraction: f1/f2 FP32 (pair-product sources), f3 as bf16 hi/lo.
 void launch_contract_tc(const DeviceSchedule& s, const float* f1, const float* f2,
                         const __nv_bfloat16* f3_split, int split_shells, int n_shells,
                         int64_t K, int64_t k_begin, int64_t k_end, int terms, double* out,
-                        int num_sms, cudaStream_t st);
+                        int num_sms, cudaStream_t st, double scale = 1.0);
 
 // Bounded-wait error flag of the tcgen05 kernel (1 = a wait expired); optionally reset.
 int tc_error_flag(bool reset);
@@ -253,6 +277,11 @@ void gridinfo_enum(bsk_plan* p, const std::vector<HostTriangle>& tri, double* nt
                    double* kmean, cudaStream_t st);
 
 void launch_scale(double* v, int64_t n, double s, cudaStream_t st);
+// A grid level's coarse spectrum from its parent plan's coarse spectrum.
+void launch_subgrid(const bsk_plan* parent, const bsk_plan* level, const cufftComplex* ps,
+                    cufftComplex* ls, cudaStream_t st);
+// Grid sizes the field synthesis compiles with constant strides (candidate grid levels).
+bool synth_fast_size(int n);
 void launch_gridinfo_finish(int64_t T, double inv_k, double* ntri, const double* s1,
                             const double* s2, const double* s3, double* kmean,
                             cudaStream_t st);

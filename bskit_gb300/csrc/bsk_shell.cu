@@ -257,6 +257,34 @@ void launch_extract(const bsk_plan* p, const cufftComplex* fine, cufftComplex* c
   BSK_CHECK_CUDA(cudaGetLastError());
 }
 
+// A grid level's coarse spectrum from its parent's: sub[a][b][c] = parent[qa mod Ngp][qb mod
+// Ngp][c] (same 1/N^3 scaling, same CIC weights), zero on the level's own Nyquist planes.
+__global__ void subgrid_kernel(int Ngp, int Ngs, const float2* __restrict__ parent,
+                               float2* __restrict__ sub) {
+  const int Hs = Ngs / 2 + 1, Hp = Ngp / 2 + 1;
+  const int64_t Mh = (int64_t)Ngs * Ngs * Hs;
+  for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < Mh;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(m % Hs);
+    const int64_t r = m / Hs;
+    const int b = (int)(r % Ngs), a = (int)(r / Ngs);
+    const int qa = fft_freq(a, Ngs), qb = fft_freq(b, Ngs);
+    float2 v = make_float2(0.f, 0.f);
+    if (!(qa == -Ngs / 2 || qb == -Ngs / 2 || c == Ngs / 2)) {
+      const int pa = qa < 0 ? qa + Ngp : qa, pb = qb < 0 ? qb + Ngp : qb;
+      v = parent[((int64_t)pa * Ngp + pb) * Hp + c];
+    }
+    sub[m] = v;
+  }
+}
+
+void launch_subgrid(const bsk_plan* parent, const bsk_plan* level, const cufftComplex* ps,
+                    cufftComplex* ls, cudaStream_t st) {
+  subgrid_kernel<<<grid_for(level->Mh, 256, level->num_sms * 16), 256, 0, st>>>(
+      parent->Ng, level->Ng, reinterpret_cast<const float2*>(ps), reinterpret_cast<float2*>(ls));
+  BSK_CHECK_CUDA(cudaGetLastError());
+}
+
 void launch_window(int N, float scale, cufftComplex* spec, const float* axis_w, int num_sms,
                    cudaStream_t st) {
   const int64_t Mh = (int64_t)N * N * (N / 2 + 1);

@@ -644,6 +644,10 @@ bool make_plan(int n, FftPlan& pl) {
 
 }  // namespace
 
+bool synth_fast_size(int n) {
+  return n == 48 || n == 96 || n == 192 || n == 256 || n == 384 || n == 480;
+}
+
 bool synth_supported(int n) {
   FftPlan pl;
   return n >= 8 && n <= 512 && n % 4 == 0 && make_plan(n, pl);
@@ -697,6 +701,7 @@ void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0
     case 48: run_synth<48>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
     case 96: run_synth<96>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
     case 192: run_synth<192>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+    case 256: run_synth<256>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
     case 384: run_synth<384>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
     case 480: run_synth<480>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
     default: run_synth<0>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;

@@ -11,7 +11,8 @@ import torch
 
 from . import _lib
 
-GRID_MODES = {"reduced": _lib.GRID_REDUCED, "native": _lib.GRID_NATIVE}
+GRID_MODES = {"reduced": _lib.GRID_REDUCED, "native": _lib.GRID_NATIVE,
+              "single": _lib.GRID_REDUCED_SINGLE}
 
 
 def _stream_ptr(stream=None):
@@ -54,6 +55,18 @@ class TriangleSet:
         _lib.call("bsk_triset_schedule", self.handle, out)
         return int(out[0]), int(out[1]), int(out[2])
 
+    def levels(self):
+        """The grid levels of the set's resident contraction: one dict per level with the
+        grid side, tiles, sum of tile columns, pair rows, bins and shells synthesised (empty
+        when every bin is contracted on the plan's grid)."""
+        n = _lib.load().bsk_triset_levels(self.handle, None, 0)
+        if n < 0:
+            raise _lib.BskError(n, _lib.last_error())
+        out = (ctypes.c_int64 * (6 * max(n, 1)))()
+        _lib.load().bsk_triset_levels(self.handle, out, n)
+        keys = ("ngrid", "tiles", "sum_nc", "pair_rows", "bins", "shells")
+        return [dict(zip(keys, (int(v) for v in out[6 * k:6 * k + 6]))) for k in range(n)]
+
     def close(self):
         if getattr(self, "handle", None):
             with torch.cuda.device(self.plan.device):
@@ -70,8 +83,10 @@ class TriangleSet:
 class Plan:
     """Engine state for one (Nmesh, BoxSize, shell list) on one device.
 
-    ``grid='reduced'`` contracts on the smallest FFT-friendly grid Ng > 3 q_max
-    (identical sums, see ``bsk_plan_create``); ``grid='native'`` uses Ng = Nmesh.
+    ``grid='reduced'`` contracts on the smallest FFT-friendly grid Ng > 3 q_max, and the bins
+    of small shells on smaller grids (identical sums, see ``bsk_plan_create`` and
+    ``bsk_triset_levels``); ``grid='single'`` keeps every bin on that one reduced grid;
+    ``grid='native'`` uses Ng = Nmesh.
     """
 
     def __init__(self, nmesh, box_size, shell_edges, grid="reduced", mem_budget=0, device=None):

@@ -61,8 +61,10 @@ enum bsk_precision {
 
 /* Real-space grid the contraction runs on. */
 enum bsk_grid_mode {
-  BSK_GRID_REDUCED = 0, /* smallest FFT-friendly Ng with Ng > 3*max|q_c| (exact: no aliasing onto the summed k=0 mode) */
-  BSK_GRID_NATIVE = 1   /* Ng = N, the mesh's own grid                                   */
+  BSK_GRID_REDUCED = 0, /* smallest FFT-friendly Ng with Ng > 3*max|q_c| (exact: no aliasing onto the summed k=0 mode);
+                           bins of small shells on smaller grids (grid levels, bsk_triset_levels) */
+  BSK_GRID_NATIVE = 1,  /* Ng = N, the mesh's own grid                                   */
+  BSK_GRID_REDUCED_SINGLE = 2 /* the reduced grid for every bin (no grid levels)          */
 };
 
 /* bsk_plan_query() fields */
@@ -132,6 +134,18 @@ int64_t bsk_triset_size(const bsk_triset* set);
  * bf16x3 (useful: 2 x T).  Diagnostics; no counterpart in the reference.
  */
 int bsk_triset_schedule(const bsk_triset* set, int64_t* out);
+/*
+ * Grid levels of a set (plans made with BSK_GRID_REDUCED): a bin (i, j, l) is contracted on
+ * the smallest chosen grid side Ng with Ng > r_i + r_j + r_l and 2 r < Ng for its shells
+ * (r = largest |q_c| of a shell mode), which is exact -- no closed triangle of shell modes
+ * wraps around such a grid -- at a cost proportional to Ng^3; the sides are chosen to
+ * minimise contraction plus field-synthesis work.  Returns the number of levels (0: one
+ * grid, the plan's) or a negative error; for the first `cap` levels, out[6k .. 6k+5] =
+ * Ng, tiles, sum of tile columns, pair rows, bins, shells synthesised.  Used by the
+ * resident bsk_measure_b(_range) path (shell streaming keeps the plan's grid).
+ * Diagnostics; no counterpart in the reference (its FFTs run on the mesh's grid).
+ */
+int bsk_triset_levels(const bsk_triset* set, int64_t* out, int cap);
 
 /*
  * Forward-transform a real mesh into field slot `slot` (0, 1, 2 = the
