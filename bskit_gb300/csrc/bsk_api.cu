@@ -590,84 +590,78 @@ void sync_level(bsk_plan* p, bsk_plan* q, int s, cudaStream_t st) {
 
 // Grid sides the levels may take (below the plan's own): the sizes whose field synthesis is
 // compiled with constant strides.
-const int kLevelSides[] = {48, 96, 192, 256, 384, 480};
+const int kLevelSides[] = {48, 96, 128, 160, 192, 240, 256, 288, 320, 384, 480};
 // Per point: one 128-row tile of the tensor-core contraction costs ~13 field syntheses of a
 // shell (measured on the 384^3 grid: 2.44 ms per tile, 0.187 ms per shell of a batch of 8).
 constexpr double kTileCost = 13.0, kShellCost = 1.0;
 
-// Chooses the set's grid levels (minimum modelled cost over the subsets of the candidate
-// sides, the plan's own grid always last) and builds one schedule per level.
+// Chooses the set's grid levels and builds one schedule per level.  Bin t can use any side
+// S > v_t = max(r_i + r_j + r_l, 2 max(r_i, r_j, r_l)) and goes to the smallest chosen one,
+// so a level's bins are those with v_t in [previous chosen side, its side): its modelled
+// cost (tiles of its schedule and the shell prefix it synthesises, times side^3) depends on
+// those two sides only, and the cheapest chain of sides ending at the plan's own grid is a
+// shortest path over the candidate sides.
 void build_levels(bsk_plan* p, bsk_triset* set) {
-  std::vector<int> cand;
+  std::vector<int> sides;  // candidates, then the plan's grid
   for (int n : kLevelSides)
-    if (n < p->Ng && synth_fast_size(n)) cand.push_back(n);
+    if (n < p->Ng && synth_fast_size(n)) sides.push_back(n);
+  sides.push_back(p->Ng);
+  const int m = (int)sides.size();
   const int nt = (int)set->u_tri.size();
-  std::vector<int> need(nt), rmax(nt);
+  std::vector<int> v(nt);
   for (int t = 0; t < nt; ++t) {
     const HostTriangle& h = set->u_tri[t];
     const int ri = p->shell_r[h.i], rj = p->shell_r[h.j], rl = p->shell_r[h.l];
-    need[t] = ri + rj + rl;
-    rmax[t] = std::max(ri, std::max(rj, rl));
+    v[t] = std::max(ri + rj + rl, 2 * std::max(ri, std::max(rj, rl)));
   }
-  auto assign = [&](const std::vector<int>& sides, std::vector<int>& lev) {
-    lev.assign(nt, (int)sides.size() - 1);
-    for (int t = 0; t < nt; ++t)
-      for (int k = 0; k + 1 < (int)sides.size(); ++k)
-        if (need[t] < sides[k] && 2 * rmax[t] < sides[k]) {
-          lev[t] = k;
-          break;
-        }
-  };
-  double best = -1.0;
-  std::vector<int> best_sides;
-  const int nc = (int)cand.size();
-  for (int mask = 0; mask < (1 << nc); ++mask) {
-    std::vector<int> sides;
-    for (int k = 0; k < nc; ++k)
-      if (mask >> k & 1) sides.push_back(cand[k]);
-    sides.push_back(p->Ng);
-    std::vector<int> lev;
-    assign(sides, lev);
-    double cost = 0.0;
-    for (int k = 0; k < (int)sides.size(); ++k) {
-      std::vector<HostTriangle> tk;
-      int top = -1;
-      for (int t = 0; t < nt; ++t)
-        if (lev[t] == k) {
-          tk.push_back(set->u_tri[t]);
-          top = std::max(top, std::max(set->u_tri[t].i, std::max(set->u_tri[t].j,
-                                                                  set->u_tri[t].l)));
-        }
-      if (tk.empty()) continue;
-      HostSchedule hs;
-      tile_schedule(tk, p->n, nullptr, hs);
-      // every level synthesises the prefix of shells its bins use
-      const double k3 = std::pow((double)sides[k], 3);
-      cost += k3 * (kTileCost * hs.tiles.size() + kShellCost * (top + 1));
-    }
-    if (best < 0 || cost < best) {
-      best = cost;
-      best_sides = sides;
-    }
-  }
-  std::vector<int> lev;
-  assign(best_sides, lev);
-  for (int k = 0; k < (int)best_sides.size(); ++k) {
-    std::vector<HostTriangle> tk;
-    std::vector<int> idx;
+  // bins with lo <= v < side (lo = 0 for the first chosen side)
+  auto members = [&](int lo, int side, std::vector<HostTriangle>* tk, std::vector<int>* idx) {
     int top = -1;
     for (int t = 0; t < nt; ++t)
-      if (lev[t] == k) {
-        tk.push_back(set->u_tri[t]);
-        idx.push_back(set->u_idx[t]);
-        top = std::max(top, std::max(set->u_tri[t].i, std::max(set->u_tri[t].j,
-                                                                set->u_tri[t].l)));
+      if (v[t] >= lo && v[t] < side) {
+        const HostTriangle& h = set->u_tri[t];
+        if (tk) tk->push_back(h);
+        if (idx) idx->push_back(set->u_idx[t]);
+        top = std::max(top, std::max(h.i, std::max(h.j, h.l)));
       }
+    return top;
+  };
+  auto cost = [&](int lo, int side) {
+    std::vector<HostTriangle> tk;
+    const int top = members(lo, side, &tk, nullptr);
+    if (tk.empty()) return 0.0;
+    HostSchedule hs;
+    tile_schedule(tk, p->n, nullptr, hs);
+    return std::pow((double)side, 3) * (kTileCost * hs.tiles.size() + kShellCost * (top + 1));
+  };
+  // best[j]: cheapest chain covering the bins with v < sides[j], ending at sides[j]
+  std::vector<double> best(m, 0.0);
+  std::vector<int> prev(m, -1);
+  for (int j = 0; j < m; ++j) {
+    best[j] = cost(0, sides[j]);
+    prev[j] = -1;
+    for (int i = 0; i < j; ++i) {
+      const double c = best[i] + cost(sides[i], sides[j]);
+      if (c < best[j]) {
+        best[j] = c;
+        prev[j] = i;
+      }
+    }
+  }
+  std::vector<int> chain;
+  for (int j = m - 1; j >= 0; j = prev[j]) chain.push_back(j);
+  std::reverse(chain.begin(), chain.end());
+  int lo = 0;
+  for (int j : chain) {
+    std::vector<HostTriangle> tk;
+    std::vector<int> idx;
+    const int top = members(lo, sides[j], &tk, &idx);
+    lo = sides[j];
     if (tk.empty()) continue;
     GridLevel lv;
     lv.n_shells = top + 1;
     lv.bins = (int64_t)tk.size();
-    lv.plan = k + 1 == (int)best_sides.size() ? p : level_plan(p, best_sides[k], top + 1);
+    lv.plan = j == m - 1 ? p : level_plan(p, sides[j], top + 1);
     set->levels.push_back(lv);
     build_schedule(tk, lv.plan->n, set->levels.back().sched, &idx);
   }

@@ -645,7 +645,13 @@ bool make_plan(int n, FftPlan& pl) {
 }  // namespace
 
 bool synth_fast_size(int n) {
-  return n == 48 || n == 96 || n == 192 || n == 256 || n == 384 || n == 480;
+  switch (n) {
+    case 48: case 96: case 128: case 160: case 192: case 240: case 256: case 288: case 320:
+    case 384: case 480:
+      return true;
+    default:
+      return false;
+  }
 }
 
 bool synth_supported(int n) {
@@ -700,8 +706,13 @@ void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0
   switch (N) {
     case 48: run_synth<48>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
     case 96: run_synth<96>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+    case 128: run_synth<128>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+    case 160: run_synth<160>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
     case 192: run_synth<192>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+    case 240: run_synth<240>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
     case 256: run_synth<256>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+    case 288: run_synth<288>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
+    case 320: run_synth<320>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
     case 384: run_synth<384>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
     case 480: run_synth<480>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
     default: run_synth<0>(A, pl, nk, Cp, ns, fft_smem, x_smem, st); break;
