@@ -222,7 +222,7 @@ void ensure_fields(bsk_plan* p, int s, cudaStream_t st, bool with_split = false,
   FieldSlot& f = p->slot[s];
   BSK_REQUIRE(f.painted, BSK_ERR_STATE, "field slot " + std::to_string(s) + " was not painted");
   const int need = n_need < 0 ? p->n : std::min(n_need, p->n);
-  if (f.fields_ok && f.fields_n >= need) return;
+  if (f.fields_ok && f.fields_n >= need && f.fields_from == 0) return;
   if (!f.fields) {
     check_budget(p, (size_t)p->n_alloc() * p->K * sizeof(float), "the shell fields");
     f.fields = (float*)dmalloc((size_t)p->n_alloc() * p->K * sizeof(float));
@@ -248,7 +248,11 @@ void ensure_fields(bsk_plan* p, int s, cudaStream_t st, bool with_split = false,
     }
     f.fields_ok = true;
     f.fields_n = done;
-    f.split_ok = with_split;
+    f.fields_from = 0;
+    if (with_split) {
+      f.split_ok = true;
+      f.split_n = done;
+    }
     return;
   }
   bind_work(p, p->c2r, st);
@@ -263,16 +267,66 @@ void ensure_fields(bsk_plan* p, int s, cudaStream_t st, bool with_split = false,
   }
   f.fields_ok = true;
   f.fields_n = p->n;
+  f.fields_from = 0;
   f.split_ok = false;
 }
 
 void ensure_split(bsk_plan* p, int s, cudaStream_t st, int n_need = -1) {
   FieldSlot& f = p->slot[s];
+  const int need = n_need < 0 ? p->n : std::min(n_need, p->n);
   ensure_fields(p, s, st, true, n_need);
-  if (f.split_ok) return;
+  if (f.split_ok && f.split_n >= need) return;
   alloc_split(p, f);
-  launch_split(f.fields, p->n_alloc(), p->K, f.split, st);
+  launch_split(f.fields, p->n_alloc(), p->K, f.split, st);  // FP32 valid from shell 0
   f.split_ok = true;
+  f.split_n = p->n;
+}
+
+// A grid level's slot for shells [0, nn): the FP32 fields of shells >= fp_from (the pair
+// factors of its bins; nn when the slot is not a pair factor) and, when `need_split`, the
+// bf16 split of all of them (the column operand), in one synthesis pass per batch; batches
+// that hold neither are skipped.
+void ensure_level_fields(bsk_plan* q, int s, cudaStream_t st, int nn, int fp_from,
+                         bool need_split) {
+  FieldSlot& f = q->slot[s];
+  BSK_REQUIRE(f.painted, BSK_ERR_STATE, "field slot " + std::to_string(s) + " was not painted");
+  nn = std::min(nn, q->n);
+  fp_from = std::min(fp_from, nn);
+  const bool fp_ok = fp_from >= nn || (f.fields_ok && f.fields_from <= fp_from &&
+                                       f.fields_n >= nn);
+  const bool split_ok = !need_split || (f.split_ok && f.split_n >= nn);
+  if (fp_ok && split_ok) return;
+  if (!f.fields) {
+    check_budget(q, (size_t)q->n_alloc() * q->K * sizeof(float), "the shell fields");
+    f.fields = (float*)dmalloc((size_t)q->n_alloc() * q->K * sizeof(float));
+    const size_t pad = (size_t)(q->n_alloc() - q->n) * q->K;
+    if (pad)
+      BSK_CHECK_CUDA(cudaMemset(f.fields + (size_t)q->n * q->K, 0, pad * sizeof(float)));
+  }
+  if (!q->synth_ws) {
+    check_budget(q, q->synth_ws_bytes, "the field-synthesis workspace");
+    q->synth_ws = dmalloc(q->synth_ws_bytes);
+    synth_init_workspace(q->Ng, q->synth_ws);
+  }
+  if (need_split) alloc_split(q, f);
+  const int from = need_split ? 0 : fp_from / q->chunk * q->chunk;
+  int done = from;
+  for (int s0 = from; s0 < nn; s0 += q->chunk) {
+    const int ns = std::min(q->chunk, q->n - s0);
+    int R = 0;
+    for (int k = s0; k < s0 + ns; ++k) R = std::max(R, q->shell_r[k]);
+    launch_synth(q->Ng, f.spec, q->table, s0, ns, R, q->synth_ws, f.fields,
+                 need_split ? f.split : nullptr, q->n_alloc(), st, 0, fp_from);
+    done = s0 + ns;
+  }
+  // what this pass wrote replaces what the slot held
+  f.fields_ok = fp_from < nn;
+  f.fields_from = fp_from;
+  f.fields_n = done;
+  if (need_split) {
+    f.split_ok = true;
+    f.split_n = done;
+  }
 }
 
 void free_slot(FieldSlot& f) {
@@ -585,7 +639,7 @@ void sync_level(bsk_plan* p, bsk_plan* q, int s, cudaStream_t st) {
   qf.gen = pf.gen;
   qf.fields_ok = false;
   qf.split_ok = false;
-  qf.fields_n = 0;
+  qf.fields_n = qf.split_n = qf.fields_from = 0;
 }
 
 // Grid sides the levels may take (below the plan's own): the sizes whose field synthesis is
@@ -660,6 +714,8 @@ void build_levels(bsk_plan* p, bsk_triset* set) {
     if (tk.empty()) continue;
     GridLevel lv;
     lv.n_shells = top + 1;
+    lv.src_min = top + 1;
+    for (const HostTriangle& h : tk) lv.src_min = std::min(lv.src_min, std::min(h.i, h.j));
     lv.bins = (int64_t)tk.size();
     lv.plan = j == m - 1 ? p : level_plan(p, sides[j], top + 1);
     set->levels.push_back(lv);
@@ -688,11 +744,19 @@ void measure_levels(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int
       if (b != a) sync_level(p, q, b, st);
       if (c != a && c != b) sync_level(p, q, c, st);
     }
-    if (tc) ensure_split(q, c, st, nn);  // first: a synthesis pass writes the split too
-    ensure_fields(q, a, st, false, nn);
-    ensure_fields(q, b, st, false, nn);
-    ensure_fields(q, c, st, false, nn);
-    if (tc) ensure_split(q, c, st, nn);
+    // tensor-core paths read FP32 fields only as pair factors (shells >= the level's smallest
+    // i or j) and the split of slot c; the SIMT paths read FP32 fields of every shell
+    const int sls[3] = {a, b, c};
+    for (int k = 0; k < 3; ++k) {
+      const int sl = sls[k];
+      if ((k >= 1 && sl == sls[0]) || (k == 2 && sl == sls[1])) continue;  // done already
+      const bool factor = sl == a || sl == b;
+      const int fp_from = !tc ? 0 : factor ? lv.src_min : nn;
+      ensure_level_fields(q, sl, st, nn, fp_from, tc && sl == c);
+    }
+    BSK_REQUIRE(q->slot[a].fields && q->slot[b].fields && q->slot[c].fields &&
+                    (!tc || q->slot[c].split),
+                BSK_ERR_STATE, "internal: a grid level's operands were not built");
     const int64_t q0 = level_point(k0, p->K, q->K), q1 = level_point(k1, p->K, q->K);
     if (q1 <= q0) continue;
     const double scale = std::pow(p->L, 6) / (double)q->K;

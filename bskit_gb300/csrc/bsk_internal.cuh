@@ -130,7 +130,9 @@ struct FieldSlot {
   __nv_bfloat16* split = nullptr; // bf16 split of the n_alloc shells, chunk-major (above)
   bool fields_ok = false;
   bool split_ok = false;
-  int fields_n = 0;               // shells [0, fields_n) of `fields` (and `split`) are valid
+  int fields_n = 0;               // the FP32 fields of shells [fields_from, fields_n) are valid
+  int fields_from = 0;            // (0 unless a grid level only needed the later shells)
+  int split_n = 0;                // the split of shells [0, split_n) is valid
   int64_t gen = 0;                // bumped by every paint (keys of streamed fields); on a grid
                                   // level's plan: the parent paint its spectrum was taken from
 };
@@ -142,6 +144,7 @@ struct GridLevel {
   bsk_plan* plan = nullptr;
   DeviceSchedule sched;   // map entries are positions in the set's output
   int n_shells = 0;       // shells [0, n_shells) the level's bins use
+  int src_min = 0;        // smallest shell of the level's bins used as a pair factor (i or j)
   int64_t bins = 0;
 };
 
@@ -240,7 +243,7 @@ size_t synth_workspace_bytes(int n, int max_r, int batch);
 void synth_init_workspace(int n, void* work);
 void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0, int ns, int R,
                   void* work, float* fields, __nv_bfloat16* split, int split_shells,
-                  cudaStream_t st, int out_s0 = 0);
+                  cudaStream_t st, int out_s0 = 0, int fields_from = 0);
 // FP32 fields [S][K] -> their chunk-major bf16 hi / lo split (split_elems(S, K) values,
 // the tail of the last chunk zeroed).
 void launch_split(const float* in, int S, int64_t K, __nv_bfloat16* split, cudaStream_t st);

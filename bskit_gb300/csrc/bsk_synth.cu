@@ -311,6 +311,7 @@ __device__ __forceinline__ int kept_index(int i, int nk, int R, int n) {
 struct SynthArgs {
   int N, H, R, nk, Cp, s0, ns;
   int out0;                // shell written at fields[0] (and hi/lo[0])
+  int fields_from;         // the FP32 field is written for shells s0 + s >= fields_from only
   const float2* spec;      // [a][b][c] slot spectrum
   const uint16_t* table;   // [a][b][c] shell codes
   float2* G;               // [s][x][bk][c]   (c < Cp)
@@ -446,7 +447,8 @@ __global__ void __launch_bounds__(kThreads, 2) synth_y_kernel(SynthArgs A, FftPl
 template <int NC>
 __device__ __forceinline__ void z_last_pass(const float2* __restrict__ src,
                                             const float2* __restrict__ tw, const FftPlan& pl,
-                                            const SynthArgs& A, int sh, int64_t row0, int y0) {
+                                            const SynthArgs& A, int sh, int64_t row0, int y0,
+                                            bool fp32) {
   constexpr int np = plan_np(NC);
   constexpr int R = plan_radix(NC, np - 1);
   constexpr int M = NC / R;
@@ -472,7 +474,7 @@ __device__ __forceinline__ void z_last_pass(const float2* __restrict__ src,
       const float2 f = odd ? make_float2(got, v[r].y) : make_float2(v[r].x, got);
       if (y < NC) {
         const int64_t pt = o + (int64_t)M * r;
-        *reinterpret_cast<float2*>(A.fields + (int64_t)sh * K + pt) = f;
+        if (fp32) *reinterpret_cast<float2*>(A.fields + (int64_t)sh * K + pt) = f;
         if (A.split) {
           const __nv_bfloat162 h = __floats2bfloat162_rn(f.x, f.y);
           const float2 fb = __bfloat1622float2(h);
@@ -551,7 +553,7 @@ __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPl
       float2* src = buf0;
       float2* dst = buf1;
       run_passes_but_last<NC, kZLines, 0, 1>(src, dst, tw, pl, cn, N - cn);
-      z_last_pass<NC>(src, tw, pl, A, sh, row0, y0);
+      z_last_pass<NC>(src, tw, pl, A, sh, row0, y0, A.s0 + s >= A.fields_from);
     } else {
       const float2* res = fft_lines<NC, kZLines>(buf0, buf1, pl, tw, cn, N - cn);
       // four consecutive z per thread: 16-byte field stores, 8-byte hi / lo stores (N % 4 == 0)
@@ -565,7 +567,8 @@ __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPl
         if (rr & 1) v = make_float4(w[0].y, w[1].y, w[2].y, w[3].y);
         else v = make_float4(w[0].x, w[1].x, w[2].x, w[3].x);
         const int64_t pt = row0 + (int64_t)y * N + z;
-        *reinterpret_cast<float4*>(A.fields + (int64_t)sh * K + pt) = v;
+        if (A.s0 + s >= A.fields_from)
+          *reinterpret_cast<float4*>(A.fields + (int64_t)sh * K + pt) = v;
         if (A.split) {
           const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y);
           const __nv_bfloat162 h23 = __floats2bfloat162_rn(v.z, v.w);
@@ -675,7 +678,7 @@ void synth_init_workspace(int N, void* work) {
 
 void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0, int ns, int R,
                   void* work, float* fields, __nv_bfloat16* split, int split_shells,
-                  cudaStream_t st, int out_s0) {
+                  cudaStream_t st, int out_s0, int fields_from) {
   FftPlan pl;
   BSK_REQUIRE(make_plan(N, pl), BSK_ERR_UNSUPPORTED, "no FFT plan for this grid size");
   R = std::min(R, N / 2);
@@ -690,6 +693,7 @@ void launch_synth(int N, const cufftComplex* spec, const uint16_t* table, int s0
   A.s0 = s0;
   A.ns = ns;
   A.out0 = out_s0;
+  A.fields_from = fields_from;
   A.spec = reinterpret_cast<const float2*>(spec);
   A.table = table;
   float2* tw = reinterpret_cast<float2*>(work);
