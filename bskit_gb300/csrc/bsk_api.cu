@@ -1,6 +1,7 @@
 // C ABI of the GB300 bispectrum engine: plans, cuFFT orchestration, dispatch.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -296,7 +297,7 @@ void ensure_level_fields(bsk_plan* q, int s, cudaStream_t st, int nn, int fp_fro
                                        f.fields_n >= nn);
   const bool split_ok = !need_split || (f.split_ok && f.split_n >= nn);
   if (fp_ok && split_ok) return;
-  if (!f.fields) {
+  if (!f.fields && fp_from < nn) {  // a column-only slot needs no FP32 fields
     check_budget(q, (size_t)q->n_alloc() * q->K * sizeof(float), "the shell fields");
     f.fields = (float*)dmalloc((size_t)q->n_alloc() * q->K * sizeof(float));
     const size_t pad = (size_t)(q->n_alloc() - q->n) * q->K;
@@ -579,12 +580,18 @@ void measure_b_stream(bsk_plan* p, const bsk_triset* set, int a, int b, int c, i
 // satisfies both for every bin; bins of small shells are contracted on smaller grids, at a
 // cost proportional to Ng^3 per point, with the shells they use synthesised on those grids.
 
-// The grid-level plan of side Ng holding shells [0, n) of p (one is made when none holds
-// enough shells).  Its spectra come from p's slots (launch_subgrid); it has no transforms of
+// The grid-level plan of side Ng of p (made on first use, holding every shell of p that
+// fits the side, at least shells [0, n)).  Its spectra come from p's slots (launch_subgrid); it has no transforms of
 // its own besides the field synthesis.
 bsk_plan* level_plan(bsk_plan* p, int Ng, int n) {
   for (bsk_plan* q : p->levels)
-    if (q->Ng == Ng && q->n >= n) return q;
+    if (q->Ng == Ng) {
+      BSK_REQUIRE(q->n >= n, BSK_ERR_STATE, "internal: a grid level lacks a shell");
+      return q;
+    }
+  // every shell that fits the side (the shells are sorted by radius): one plan per side
+  // serves every triangle set of the plan
+  while (n < p->n && 2 * p->shell_r[n] < Ng) ++n;
   std::unique_ptr<bsk_plan, void (*)(bsk_plan*)> q(new bsk_plan(), destroy_plan);
   q->device = p->device;
   q->num_sms = p->num_sms;
@@ -648,6 +655,7 @@ const int kLevelSides[] = {48, 96, 128, 160, 192, 240, 256, 288, 320, 384, 480};
 // Per point: one 128-row tile of the tensor-core contraction costs ~13 field syntheses of a
 // shell (measured on the 384^3 grid: 2.44 ms per tile, 0.187 ms per shell of a batch of 8).
 constexpr double kTileCost = 13.0, kShellCost = 1.0;
+constexpr double kMinLevelPoints = 0.4;
 
 // Chooses the set's grid levels and builds one schedule per level.  Bin t can use any side
 // S > v_t = max(r_i + r_j + r_l, 2 max(r_i, r_j, r_l)) and goes to the smallest chosen one,
@@ -656,9 +664,16 @@ constexpr double kTileCost = 13.0, kShellCost = 1.0;
 // those two sides only, and the cheapest chain of sides ending at the plan's own grid is a
 // shortest path over the candidate sides.
 void build_levels(bsk_plan* p, bsk_triset* set) {
+  // A bin's rounding error relative to its value falls as 1/sqrt(points summed), so a level
+  // keeps at least kMinLevelPoints of the plan grid's points: its bins' relative errors stay
+  // within 1.6x of the plan grid's.  (BSK_LEVEL_MIN_POINTS overrides the fraction.)
+  double min_points = kMinLevelPoints;
+  if (const char* e = std::getenv("BSK_LEVEL_MIN_POINTS")) min_points = std::atof(e);
   std::vector<int> sides;  // candidates, then the plan's grid
   for (int n : kLevelSides)
-    if (n < p->Ng && synth_fast_size(n)) sides.push_back(n);
+    if (n < p->Ng && synth_fast_size(n) &&
+        std::pow((double)n / p->Ng, 3) >= min_points)
+      sides.push_back(n);
   sides.push_back(p->Ng);
   const int m = (int)sides.size();
   const int nt = (int)set->u_tri.size();
@@ -754,8 +769,8 @@ void measure_levels(bsk_plan* p, const bsk_triset* set, int a, int b, int c, int
       const int fp_from = !tc ? 0 : factor ? lv.src_min : nn;
       ensure_level_fields(q, sl, st, nn, fp_from, tc && sl == c);
     }
-    BSK_REQUIRE(q->slot[a].fields && q->slot[b].fields && q->slot[c].fields &&
-                    (!tc || q->slot[c].split),
+    BSK_REQUIRE(q->slot[a].fields && q->slot[b].fields &&
+                    (tc ? q->slot[c].split != nullptr : q->slot[c].fields != nullptr),
                 BSK_ERR_STATE, "internal: a grid level's operands were not built");
     const int64_t q0 = level_point(k0, p->K, q->K), q1 = level_point(k1, p->K, q->K);
     if (q1 <= q0) continue;

@@ -22,14 +22,15 @@
 //     A-operand ring (lane = GEMM row);
 //   * warp 1 runs the stage loop and one elected lane issues, per 16-point K step,
 //     tcgen05.mma kind::f16 with A from TMEM and B from SMEM: hi x [Bhi; Blo]
-//     (N = 2 nc: one MMA yields both hi*Bhi and hi*Blo) and, for bf16x3, lo x Bhi
-//     (N = nc rounded up to the MMA's multiple of 16, into the hi*Bhi columns; when
-//     nc is an odd multiple of 8 the last 8 of those N columns are lo x Blo of the
-//     first 8 column shells, landing on their hi*Blo sums: an extra, exact term).  The tensor core's FP32 accumulate
+//     (N = 2 nc: one MMA yields both hi*Bhi and hi*Blo) and, for bf16x3, lo x [Bhi; Blo]
+//     into the same columns (lo*Bhi onto hi*Bhi, lo*Blo onto hi*Blo): all four cross
+//     products of the two-term splits.  The tensor pipe is not this kernel's limit, so the
+//     fourth product (lo x Blo, below 2^-18 of a term) costs ~3% of the contraction and
+//     narrows the tail of the per-bin errors.  The tensor core's FP32 accumulate
 //     truncates, so an accumulator is only ever fed one stage (16 MMAs) before it is
 //     handed over;
 //   * warps 2..9 (2 per lane quadrant, 32 columns each) drain each finished
-//     accumulator with tcgen05.ld (hi*B + lo*Bhi columns and hi*Blo columns),
+//     accumulator with tcgen05.ld (hi*Bhi + lo*Bhi columns and hi*Blo + lo*Blo columns),
 //     add it into per-thread FP32 registers (round-to-nearest), and at the end
 //     of the slice add the entries that are triangle bins into the FP64 output
 //     (atomics).
@@ -64,7 +65,7 @@ constexpr int AGW = 4;
 constexpr int NUM_WARPS = 10 + 4 * AGW;       // producer, MMA, 8 drain, 4 AGW A-operand
 constexpr int THREADS = NUM_WARPS * 32;
 constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t ACC_COL = 0;               // accumulator b at 128 b: [0,nc) hi*Bhi+lo*Bhi, [nc,2nc) hi*Blo
+constexpr uint32_t ACC_COL = 0;               // accumulator b at 128 b: [0,nc) hi*Bhi+lo*Bhi, [nc,2nc) hi*Blo+lo*Blo
 constexpr uint32_t A_COL = 256;               // A stage a at 256 + 128 a: hi +0..63, lo +64..127
 // Points per work item: 32 768 when that still gives every SM at least kMinItemsPerSm
 // items (one CTA per SM walks them), else 16 384.  Longer slices spread the per-item
@@ -454,13 +455,12 @@ __global__ void __launch_bounds__(THREADS, 1)
       const TileDesc td = tiles[item % n_tiles];
       const int64_t x_begin = k_begin + sl * slice;
       const int64_t x_end = min(k_end, x_begin + slice);
-      // hi x [Bhi; Blo] (the lo rows of a block sit right after its nc hi rows), lo x Bhi.
-      // N is a multiple of 16: an N = nc MMA with nc an odd multiple of 8 also covers the
-      // first 8 lo rows (accumulated into hi*Blo columns the drain adds anyway, or never read)
+      // hi x [Bhi; Blo] and lo x [Bhi; Blo] (the lo rows of a block sit right after its nc
+      // hi rows; N = 2 nc, a multiple of 16).  bf16 (one term): hi x Bhi, N = nc rounded up
+      // to 16 (with nc an odd multiple of 8 the last 8 columns take lo rows, never read).
       const int n16 = (td.nc + 15) & ~15;
       const uint32_t kb_bytes = 2u * td.nc * 128u;
       const uint32_t idesc_stack = idesc_bf16(terms >= 3 ? 2 * td.nc : n16);
-      const uint32_t idesc_hi = idesc_bf16(n16);
       for (int64_t x = x_begin; x < x_end; x += KCH, ++chunk) {
         // a fresh accumulator per stage, once the drain has emptied it
         const uint32_t b = grp % NACC;
@@ -485,7 +485,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           for (int k = 0; k < KCH / 16; ++k) {
             const uint64_t bdesc = desc_sw128(st + (k >> 2) * kb_bytes + 32 * (k & 3));
             mma_ts(d_tmem, a_hi + 8 * k, bdesc, idesc_stack, accum);
-            if (terms >= 3) mma_ts(d_tmem, a_lo + 8 * k, bdesc, idesc_hi, 1);
+            if (terms >= 3) mma_ts(d_tmem, a_lo + 8 * k, bdesc, idesc_stack, 1);
             accum = 1;
           }
           tc_commit(&bars->done[chunk % DONE_RING]);

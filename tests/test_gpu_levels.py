@@ -9,6 +9,8 @@ fields carry their own FFT rounding, so even FP64 contractions agree only to tha
 the bound is the oracle tests' FP64 bound, 2e-6 of the bin's absolute sum, and for bf16x3
 that plus its own bound (tests/test_gpu_parity.py, 4e-6).
 """
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -39,6 +41,19 @@ def _abs_sum(plan, ts, box, slots):
             * (box ** 6 / float(ng) ** 3)).cpu().numpy()
 
 
+@pytest.fixture
+def small_levels():
+    """Levels of any side: the default rule keeps only sides with >= 40% of the plan grid's
+    points (relative rounding errors within 1.6x); these tests want the small ones too."""
+    old = os.environ.get("BSK_LEVEL_MIN_POINTS")
+    os.environ["BSK_LEVEL_MIN_POINTS"] = "0"
+    yield
+    if old is None:
+        del os.environ["BSK_LEVEL_MIN_POINTS"]
+    else:
+        os.environ["BSK_LEVEL_MIN_POINTS"] = old
+
+
 def _shell_r(edges, box):
     kf = TWO_PI / box
     return [int(np.floor(hi / kf * (1.0 + 1e-9))) for _, hi in edges]
@@ -46,7 +61,7 @@ def _shell_r(edges, box):
 
 @pytest.mark.parametrize("n,box,kmax_kf,num_fields", [(128, 250.0, 32, 1), (256, 500.0, 64, 1),
                                                        (256, 500.0, 64, 2)])
-def test_levels_equal_the_single_grid(cuda, n, box, kmax_kf, num_fields):
+def test_levels_equal_the_single_grid(cuda, small_levels, n, box, kmax_kf, num_fields):
     edges, tri = _case(n, box, kmax_kf, 2, num_fields)
     slots = (0, 0, 1) if num_fields == 2 else (0, 0, 0)
     lev = Plan(n, box, edges)              # grid levels
@@ -96,7 +111,7 @@ def test_levels_equal_the_single_grid(cuda, n, box, kmax_kf, num_fields):
     one.close()
 
 
-def test_level_point_ranges_sum_to_the_whole(cuda):
+def test_level_point_ranges_sum_to_the_whole(cuda, small_levels):
     n, box = 256, 500.0
     edges, tri = _case(n, box, 64, 2)
     p = Plan(n, box, edges)
@@ -112,4 +127,16 @@ def test_level_point_ranges_sum_to_the_whole(cuda):
                     for a, b in zip(cuts[:-1], cuts[1:]))
         p.sync_check()
         assert np.abs(parts - whole).max() <= tol * np.abs(whole).max(), prec
+    p.close()
+
+
+def test_default_levels_keep_most_of_the_grid(cuda):
+    # the 512^3 headline binning: every level keeps >= 40% of the plan grid's points
+    n, box = 512, 1000.0
+    edges, tri = _case(n, box, 128, 2)
+    p = Plan(n, box, edges)
+    levels = p.triangles(tri).levels()
+    assert levels and levels[-1]["ngrid"] == p.ngrid
+    assert all(lv["ngrid"] ** 3 >= 0.4 * p.ngrid ** 3 for lv in levels)
+    assert sum(lv["bins"] for lv in levels) == len(tri)
     p.close()
