@@ -427,13 +427,14 @@ def run_ours(args):
               "frac": issued_flops / (c_ms / 1e3) / 1e12 / peak,
               "tiles": tiles, "sum_nc": sum_nc, "pair_rows": pair_rows,
               "useful_fraction": useful}
-    traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "contract_tc_traffic.json")) as f:
-            tr = json.load(f)
-        traffic = tr.get("bytes_per_launch", {}).get(args.workload)
-    except Exception:
-        pass
+    traffic = None  # the committed DRAM capture is of a single-grid launch
+    if not levels:
+        try:
+            with open(os.path.join(ROOT, "profiles", "contract_tc_traffic.json")) as f:
+                tr = json.load(f)
+            traffic = tr.get("bytes_per_launch", {}).get(args.workload)
+        except Exception:
+            pass
 
     # ---- plain FP32 path on the same workload, and agreement with it
     fp32 = None
