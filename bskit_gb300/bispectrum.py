@@ -48,8 +48,10 @@ class FFTBispectrum(object):
 
     Extra keyword arguments beyond bskit's:
     precision : 'bf16x3' (default), 'fp32', 'bf16' or 'fp64' -- arithmetic of the
-        triple-product contraction of B (grid information always uses FP64);
-    grid : 'reduced' (default) or 'native' -- see ``engine.Plan``;
+        triple-product contraction of B (grid information is exact: integer lattice
+        enumeration, or FP64 fields where that does not apply);
+    grid : 'reduced' (default: each bin on the smallest exact grid its shells allow),
+        'single' (the reduced grid for every bin) or 'native' -- see ``engine.Plan``;
     device : CUDA device of the computation;
     mem_budget : bytes of device memory the engine plan may hold (0 = no limit); a
         measurement that would exceed it raises BskError (BSK_ERR_OOM) before allocating.
