@@ -89,6 +89,9 @@ def parse():
     ap.add_argument("--no-studies", action="store_true",
                     help="skip the 512^3 cross precision study and the 1024^3 resident / "
                          "streamed runs that the headline line carries")
+    ap.add_argument("--grid", default="reduced", choices=["reduced", "single", "native"],
+                    help="contraction grid of the headline plan: reduced (grid levels), "
+                         "single (the reduced grid for every bin) or native")
     ap.add_argument("--no-cold", action="store_true",
                     help="profiling runs only: skip the one-off FP64 grid information and "
                          "normalise by 1 (same kernels and timings in the step)")
@@ -275,7 +278,7 @@ def run_ours(args):
             dist.barrier()
 
     edges, tri = workload_bins(args.workload)
-    plan = Plan(NMESH, BOX, edges, grid="reduced", device=dev)
+    plan = Plan(NMESH, BOX, edges, grid=args.grid, device=dev)
     ts = plan.triangles(tri)
     # replicas measure their own meshes; shards split one mesh's bispectrum
     seed = 1 if args.shard else 1 + rank
@@ -525,6 +528,8 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "workload_name": args.workload, "nmesh": NMESH,
                    "box": BOX, "n_shells": len(edges),
                    "n_bins": int(len(tri)), "precision": prec, "contraction_grid": ng,
+                   "grid_mode": args.grid,
+                   "grid_levels": [lv["ngrid"] for lv in ts.levels()],
                    "l2": "inputs larger than L2 (mesh %d MiB, shell fields %.1f GiB)"
                          % (NMESH ** 3 * 4 >> 20, len(edges) * ng ** 3 * 4 / 2 ** 30),
                    "parallelism": ("point-range shards of one bispectrum over %d GPUs, NCCL "
