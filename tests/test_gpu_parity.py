@@ -154,6 +154,23 @@ def test_fields_match_oracle_native_192(cuda):
         assert np.abs(f - of[s]).max() <= 1e-5 * scale, s
 
 
+@pytest.mark.parametrize("n", [128, 160, 240, 256, 288, 320])
+def test_fields_match_oracle_grid_level_sizes(cuda, n):
+    # the compile-time plans that grid levels use besides 48 / 96 / 192 / 384 / 480
+    # (16x8, 16x2x5, 16x3x5, 16x16, 16x6x3, 16x4x5), shells out to 0.45 N -- a level holds
+    # shells of radius up to nearly half its side
+    n, box, edges, _ = _small(n, 100.0, n // 12, 0.45)
+    delta = synthetic.lognormal_mesh(n, box, seed=17)
+    plan = Plan(n, box, edges, grid="native")
+    plan.paint(0, torch.from_numpy(delta))
+    of = O.shell_fields(O.spectrum(delta), n, box, edges)
+    for s in range(len(edges)):
+        f = plan.field(0, s).cpu().numpy().astype(np.float64)
+        scale = np.abs(of[s]).max()
+        assert np.abs(f - of[s]).max() <= 1e-5 * scale, s
+    plan.close()
+
+
 def test_paint_keeps_input(cuda):
     n, box, edges, _ = _small(32, 100.0, 2)
     delta = torch.from_numpy(synthetic.lognormal_mesh(n, box, seed=12)).cuda()
