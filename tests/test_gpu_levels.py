@@ -18,6 +18,7 @@ import torch
 from bskit_gb300 import bins as B
 from bskit_gb300 import synthetic
 from bskit_gb300.engine import Plan
+from bskit_gb300.serving import bin_lists
 
 pytestmark = pytest.mark.gpu
 
@@ -140,3 +141,45 @@ def test_default_levels_keep_most_of_the_grid(cuda):
     assert all(lv["ngrid"] ** 3 >= 0.4 * p.ngrid ** 3 for lv in levels)
     assert sum(lv["bins"] for lv in levels) == len(tri)
     p.close()
+
+
+@pytest.mark.parametrize("kind,num_fields", [("equilateral", 1), ("isosceles", 1),
+                                             ("squeezed", 1), ("equilateral", 2),
+                                             ("squeezed", 2)])
+@pytest.mark.parametrize("min_points", ["0", None])
+def test_bin_sets_on_levels_equal_the_single_grid(cuda, kind, num_fields, min_points):
+    # the serving mix's bin sets (auto and cross) on grid levels, with the default 40% rule
+    # and with levels of any side
+    n, box = 256, 500.0
+    kf = TWO_PI / box
+    spec = dict(kmin=kf, kmax=64 * kf, dk=2 * kf, triangle_type=kind, squeezed_bin_index=0)
+    edges, tri = bin_lists(spec, num_fields)
+    tri = np.ascontiguousarray(tri, dtype=np.int32)
+    slots = (0, 0, 1) if num_fields == 2 else (0, 0, 0)
+    old = os.environ.get("BSK_LEVEL_MIN_POINTS")
+    if min_points is not None:
+        os.environ["BSK_LEVEL_MIN_POINTS"] = min_points
+    try:
+        lev = Plan(n, box, edges)
+        ts_l = lev.triangles(tri)
+    finally:
+        if old is None:
+            os.environ.pop("BSK_LEVEL_MIN_POINTS", None)
+        else:
+            os.environ["BSK_LEVEL_MIN_POINTS"] = old
+    one = Plan(n, box, edges, grid="single")
+    ts_1 = one.triangles(tri)
+    d1 = synthetic.lognormal_mesh_torch(n, box, seed=5, device=cuda).contiguous()
+    meshes = [d1] if num_fields == 1 else [d1, (0.7 * d1 + 0.2 * torch.randn_like(d1))]
+    for p in (lev, one):
+        for s_, m in enumerate(meshes):
+            p.paint(s_, m.contiguous())
+    b64_1 = one.measure_b(ts_1, slots=slots, precision="fp64").cpu().numpy()
+    babs = _abs_sum(one, ts_1, box, slots)
+    live = babs > 0
+    for prec, bound in (("fp64", 2e-6), ("bf16x3", 6e-6)):
+        b = lev.measure_b(ts_l, slots=slots, precision=prec).cpu().numpy()
+        lev.sync_check()
+        assert np.all(np.abs(b - b64_1)[live] <= bound * babs[live]), (prec, ts_l.levels())
+    lev.close()
+    one.close()
