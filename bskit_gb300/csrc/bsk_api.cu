@@ -657,12 +657,8 @@ const int kLevelSides[] = {48, 96, 128, 160, 192, 240, 256, 288, 320, 384, 480};
 constexpr double kTileCost = 13.0, kShellCost = 1.0;
 constexpr double kMinLevelPoints = 0.4;
 
-// Chooses the set's grid levels and builds one schedule per level.  Bin t can use any side
-// S > v_t = max(r_i + r_j + r_l, 2 max(r_i, r_j, r_l)) and goes to the smallest chosen one,
-// so a level's bins are those with v_t in [previous chosen side, its side): its modelled
-// cost (tiles of its schedule and the shell prefix it synthesises, times side^3) depends on
-// those two sides only, and the cheapest chain of sides ending at the plan's own grid is a
-// shortest path over the candidate sides.
+// Chooses the set's grid levels (choose_level_sides over the candidate sides) and builds one
+// schedule per level, a level plan for every side below the plan's own.
 void build_levels(bsk_plan* p, bsk_triset* set) {
   // A bin's rounding error relative to its value falls as 1/sqrt(points summed), so a level
   // keeps at least kMinLevelPoints of the plan grid's points: its bins' relative errors stay
@@ -677,55 +673,19 @@ void build_levels(bsk_plan* p, bsk_triset* set) {
   sides.push_back(p->Ng);
   const int m = (int)sides.size();
   const int nt = (int)set->u_tri.size();
-  std::vector<int> v(nt);
-  for (int t = 0; t < nt; ++t) {
-    const HostTriangle& h = set->u_tri[t];
-    const int ri = p->shell_r[h.i], rj = p->shell_r[h.j], rl = p->shell_r[h.l];
-    v[t] = std::max(ri + rj + rl, 2 * std::max(ri, std::max(rj, rl)));
-  }
-  // bins with lo <= v < side (lo = 0 for the first chosen side)
-  auto members = [&](int lo, int side, std::vector<HostTriangle>* tk, std::vector<int>* idx) {
-    int top = -1;
-    for (int t = 0; t < nt; ++t)
-      if (v[t] >= lo && v[t] < side) {
-        const HostTriangle& h = set->u_tri[t];
-        if (tk) tk->push_back(h);
-        if (idx) idx->push_back(set->u_idx[t]);
-        top = std::max(top, std::max(h.i, std::max(h.j, h.l)));
-      }
-    return top;
-  };
-  auto cost = [&](int lo, int side) {
-    std::vector<HostTriangle> tk;
-    const int top = members(lo, side, &tk, nullptr);
-    if (tk.empty()) return 0.0;
-    HostSchedule hs;
-    tile_schedule(tk, p->n, nullptr, hs);
-    return std::pow((double)side, 3) * (kTileCost * hs.tiles.size() + kShellCost * (top + 1));
-  };
-  // best[j]: cheapest chain covering the bins with v < sides[j], ending at sides[j]
-  std::vector<double> best(m, 0.0);
-  std::vector<int> prev(m, -1);
+  const std::vector<int> lev =
+      choose_level_sides(set->u_tri, p->shell_r, sides, p->n, kTileCost, kShellCost);
   for (int j = 0; j < m; ++j) {
-    best[j] = cost(0, sides[j]);
-    prev[j] = -1;
-    for (int i = 0; i < j; ++i) {
-      const double c = best[i] + cost(sides[i], sides[j]);
-      if (c < best[j]) {
-        best[j] = c;
-        prev[j] = i;
-      }
-    }
-  }
-  std::vector<int> chain;
-  for (int j = m - 1; j >= 0; j = prev[j]) chain.push_back(j);
-  std::reverse(chain.begin(), chain.end());
-  int lo = 0;
-  for (int j : chain) {
     std::vector<HostTriangle> tk;
     std::vector<int> idx;
-    const int top = members(lo, sides[j], &tk, &idx);
-    lo = sides[j];
+    int top = -1;
+    for (int t = 0; t < nt; ++t)
+      if (lev[t] == j) {
+        const HostTriangle& h = set->u_tri[t];
+        tk.push_back(h);
+        idx.push_back(set->u_idx[t]);
+        top = std::max(top, std::max(h.i, std::max(h.j, h.l)));
+      }
     if (tk.empty()) continue;
     GridLevel lv;
     lv.n_shells = top + 1;

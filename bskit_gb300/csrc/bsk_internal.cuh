@@ -95,6 +95,12 @@ void tile_schedule(const std::vector<HostTriangle>& tri, int n_shells,
                    const std::vector<int>* map_index, HostSchedule& out);
 
 // tile_schedule, uploaded to the device (with the SIMT kernels' sub-tile list).
+// Grid levels of a triangle set: per triangle the index in `sides` (ascending, the plan's
+// own grid last) of the side it is contracted on (host only, bsk_schedule.cu).
+std::vector<int> choose_level_sides(const std::vector<HostTriangle>& tri,
+                                    const std::vector<int>& shell_r,
+                                    const std::vector<int>& sides, int n_shells,
+                                    double tile_cost, double shell_cost);
 void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSchedule& out,
                     const std::vector<int>* map_index = nullptr);
 

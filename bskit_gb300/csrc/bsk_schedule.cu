@@ -14,6 +14,7 @@
 // [c][r] -> t scatters tile entries back to triangle bins (-1 for entries that
 // are not bins).
 #include <algorithm>
+#include <cmath>
 #include <map>
 
 #include "bsk_internal.cuh"
@@ -181,6 +182,67 @@ void tile_schedule(const std::vector<HostTriangle>& tri, int n_shells,
     tiles.push_back(d);
   }
   out.sum_nc = sum_nc;
+}
+
+// Grid levels of a triangle set (host only).  Bin t can use any side S > v_t =
+// max(r_i + r_j + r_l, 2 max(r_i, r_j, r_l)) (no closed triangle of its modes wraps around,
+// its shells fit the Nyquist range) and goes to the smallest chosen side, so a level's bins
+// are those with v_t in [previous chosen side, its side): its modelled cost -- side^3 x
+// (tile_cost x tiles of its schedule + shell_cost x the shell prefix it synthesises) --
+// depends on those two sides only, and the cheapest chain of sides ending at the last one
+// (the plan's own grid, which holds every bin) is a shortest path over the candidates.
+// Returns, per triangle, the index in `sides` of its side.
+std::vector<int> choose_level_sides(const std::vector<HostTriangle>& tri,
+                                    const std::vector<int>& shell_r,
+                                    const std::vector<int>& sides, int n_shells,
+                                    double tile_cost, double shell_cost) {
+  const int m = (int)sides.size();
+  const int nt = (int)tri.size();
+  BSK_REQUIRE(m >= 1, BSK_ERR_STATE, "internal: no grid side");
+  std::vector<int> v(nt);
+  for (int t = 0; t < nt; ++t) {
+    const HostTriangle& h = tri[t];
+    const int ri = shell_r[h.i], rj = shell_r[h.j], rl = shell_r[h.l];
+    v[t] = std::max(ri + rj + rl, 2 * std::max(ri, std::max(rj, rl)));
+    BSK_REQUIRE(v[t] < sides[m - 1], BSK_ERR_STATE, "internal: a bin exceeds the plan's grid");
+  }
+  // modelled cost of the level of side `side` holding the bins with lo <= v < side
+  auto cost = [&](int lo, int side) {
+    std::vector<HostTriangle> tk;
+    int top = -1;
+    for (int t = 0; t < nt; ++t)
+      if (v[t] >= lo && v[t] < side) {
+        tk.push_back(tri[t]);
+        top = std::max(top, std::max(tri[t].i, std::max(tri[t].j, tri[t].l)));
+      }
+    if (tk.empty()) return 0.0;
+    HostSchedule hs;
+    tile_schedule(tk, n_shells, nullptr, hs);
+    return std::pow((double)side, 3) * (tile_cost * hs.tiles.size() + shell_cost * (top + 1));
+  };
+  // best[j]: cheapest chain covering the bins with v < sides[j], ending at sides[j]
+  std::vector<double> best(m, 0.0);
+  std::vector<int> prev(m, -1);
+  for (int j = 0; j < m; ++j) {
+    best[j] = cost(0, sides[j]);
+    for (int i = 0; i < j; ++i) {
+      const double c = best[i] + cost(sides[i], sides[j]);
+      if (c < best[j]) {
+        best[j] = c;
+        prev[j] = i;
+      }
+    }
+  }
+  std::vector<int> chain;
+  for (int j = m - 1; j >= 0; j = prev[j]) chain.push_back(j);
+  std::vector<int> lev(nt, m - 1);
+  for (int t = 0; t < nt; ++t)
+    for (int k = (int)chain.size() - 1; k >= 0; --k)  // chain is largest side first
+      if (v[t] < sides[chain[k]]) {
+        lev[t] = chain[k];
+        break;
+      }
+  return lev;
 }
 
 void build_schedule(const std::vector<HostTriangle>& tri, int n_shells, DeviceSchedule& out,

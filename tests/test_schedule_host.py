@@ -101,3 +101,55 @@ def test_more_than_64_shells_cut_rows(harness, tmp_path):
     tri80 = ([(79, 79, l) for l in range(80)] + [(70, 5, l) for l in range(0, 80, 2)] +
              [(10, 12, l) for l in range(0, 80, 7)] + [(0, 0, 0)])
     assert sum(d["nrows"] for d in schedule(harness, tmp_path, 80, tri80)) == 7
+
+
+def level_choice(exe, tmp_path, shell_r, sides, tri):
+    tri = np.asarray(tri, dtype=int).reshape(-1, 3)
+    path = tmp_path / "lev.txt"
+    with open(path, "w") as f:
+        f.write("%d %d %d\n" % (len(shell_r), len(tri), len(sides)))
+        f.write(" ".join(map(str, shell_r)) + "\n" + " ".join(map(str, sides)) + "\n")
+        f.writelines("%d %d %d\n" % tuple(t) for t in tri)
+    out = subprocess.run([exe, "levels", str(path)], check=True, capture_output=True,
+                         text=True).stdout.splitlines()
+    assert not out[0].startswith("error"), out[0]
+    lev = np.array([int(line.split()[2]) for line in out if line.startswith("lev ")])
+    cost = {(int(a), int(b)): float(c) for _, a, b, c in
+            (line.split() for line in out if line.startswith("cost "))}
+    return lev, cost
+
+
+def _chain_cost(cost, chosen):
+    prev, total = -1, 0.0
+    for j in sorted(chosen):
+        total += cost[(prev, j)]
+        prev = j
+    return total
+
+
+@pytest.mark.parametrize("case", ["headline", "mesh256", "cross256"])
+def test_grid_level_sides_exact_and_cheapest(harness, tmp_path, case):
+    # the level choice of the plan's resident contraction (bsk_triset_create): every bin on a
+    # side above max(r_i + r_j + r_l, 2 max r) -- exact -- on the smallest chosen such side,
+    # and the chosen chain as cheap as any subset of the candidate sides
+    import itertools
+    import math
+    n, box, kmax, nf, top = {"headline": (512, 1000.0, 128, 1, 384),
+                             "mesh256": (256, 500.0, 64, 1, 192),
+                             "cross256": (256, 500.0, 64, 2, 192)}[case]
+    kf = 2 * math.pi / box
+    kw = dict(kmin=kf, kmax=kmax * kf, dk=2 * kf)
+    edges = B.generate_bin_edge_list(**kw)
+    tri = np.unique(B.generate_triangle_bin_list(num_fields=nf, return_indices=True, **kw), axis=0)
+    r = [int(np.floor(hi / kf * (1.0 + 1e-9))) for _, hi in edges]
+    sides = [s for s in (48, 96, 128, 160, 192, 240, 256, 288, 320, 384, 480) if s < top] + [top]
+    lev, cost = level_choice(harness, tmp_path, r, sides, tri)
+    v = np.array([max(r[a] + r[b] + r[c], 2 * max(r[a], r[b], r[c])) for a, b, c in tri])
+    side = np.array(sides)[lev]
+    assert np.all(side > v)
+    chosen = sorted(set(lev.tolist()))
+    for t in range(len(tri)):  # no smaller chosen side holds the bin
+        assert not any(sides[k] > v[t] and sides[k] < side[t] for k in chosen)
+    best = min(_chain_cost(cost, list(sub) + [len(sides) - 1])
+               for k in range(len(sides)) for sub in itertools.combinations(range(len(sides) - 1), k))
+    assert _chain_cost(cost, chosen) <= best * (1 + 1e-12)
