@@ -12,8 +12,8 @@
 //           when asked, as the bf16 hi / lo planes of the tensor-core contraction.
 // Every array keeps q_c fastest, so the passes read and write 8- or 16-wide (64- or 128-byte)
 // runs of it.
-// The FFTs are radix-8/4/2/3/5 Stockham passes in shared memory (twiddles from a table
-// computed in double precision on the host); unnormalised, sign +1, as cuFFT's C2R.
+// The FFTs are radix-16/24/12/8/6/4/2/3/5 Stockham passes in shared memory (twiddles from a
+// table computed in double precision on the host); unnormalised, sign +1, as cuFFT's C2R.
 #include <atomic>
 #include <cmath>
 
