@@ -440,17 +440,26 @@ __global__ void __launch_bounds__(kThreads, 2) synth_y_kernel(SynthArgs A, FftPl
   }
 }
 
+// Radix of the last pass of a compile-time length, and the size of its twiddle table twl.
+template <int NC>
+__host__ __device__ constexpr int z_last_radix() { return plan_radix(NC, plan_np(NC) - 1); }
+template <int NC>
+__host__ __device__ constexpr int z_twl_size() { return NC - NC / z_last_radix<NC>(); }
+
 // Last FFT pass of the Z pass fused with its stores.  Butterfly j of a line yields the
 // outputs z = j + M r (M = n / R); lanes j (even) and j + 1 hold z and z + 1, so one
 // exchange gives the even lane row y1's pair (z, z + 1) (real parts) and the odd lane row
 // y2's (imaginary parts): 8-byte field stores, 4-byte hi / lo stores, 32-byte sectors.
+// Consecutive lanes take consecutive j, so the twiddles come from a table twl[(r - 1) M + j]
+// = e^{+2 pi i r j / n}: a warp reads consecutive entries (tw[r j] would be r apart, a
+// gcd(r, 16)-way bank conflict).
 template <int NC>
 __device__ __forceinline__ void z_last_pass(const float2* __restrict__ src,
-                                            const float2* __restrict__ tw, const FftPlan& pl,
+                                            const float2* __restrict__ twl, const FftPlan& pl,
                                             const SynthArgs& A, int sh, int64_t row0, int y0,
                                             bool fp32) {
   constexpr int np = plan_np(NC);
-  constexpr int R = plan_radix(NC, np - 1);
+  constexpr int R = z_last_radix<NC>();
   constexpr int M = NC / R;
   static_assert(np >= 2 && M % 2 == 0 && (kZLines * M) % kThreads == 0,
                 "the fused last pass wants full warps of line-ordered butterfly pairs");
@@ -462,7 +471,7 @@ __device__ __forceinline__ void z_last_pass(const float2* __restrict__ src,
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = in[j + r * M];
 #pragma unroll
-    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * j]);
+    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], twl[(r - 1) * M + j]);
     dft_radix<R>(v, pl);
     const bool odd = j & 1;
     const int y = y0 + 2 * line + (odd ? 1 : 0);
@@ -496,8 +505,14 @@ __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPl
   float2* buf0 = sm;
   float2* buf1 = buf0 + kZLines * ls;
   float2* tw = buf1 + kZLines * ls;
+  float2* twl = tw + N;  // the last pass's twiddles (compile-time lengths)
   const int ny = (N + 2 * kZLines - 1) / (2 * kZLines);
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = A.tw[i];
+  if constexpr (NC != 0) {
+    constexpr int M = NC / z_last_radix<NC>();
+    for (int i = threadIdx.x; i < z_twl_size<NC>(); i += blockDim.x)
+      twl[i] = A.tw[(i / M + 1) * (i % M)];  // r j < R M = n
+  }
   const int cn = min(A.R, N / 2) + 1;  // q_c = 0 .. cn - 1 can be nonzero
   // kThreads / kZLines threads per line, q_c strided by that
   constexpr int tpl = kThreads / kZLines;
@@ -553,7 +568,7 @@ __global__ void __launch_bounds__(kThreads, 2) synth_z_kernel(SynthArgs A, FftPl
       float2* src = buf0;
       float2* dst = buf1;
       run_passes_but_last<NC, kZLines, 0, 1>(src, dst, tw, pl, cn, N - cn);
-      z_last_pass<NC>(src, tw, pl, A, sh, row0, y0, A.s0 + s >= A.fields_from);
+      z_last_pass<NC>(src, twl, pl, A, sh, row0, y0, A.s0 + s >= A.fields_from);
     } else {
       const float2* res = fft_lines<NC, kZLines>(buf0, buf1, pl, tw, cn, N - cn);
       // four consecutive z per thread: 16-byte field stores, 8-byte hi / lo stores (N % 4 == 0)
@@ -611,7 +626,8 @@ void run_synth(const SynthArgs& A, const FftPlan& pl, int nk, int Cp, int ns, si
   // persistent Y and Z passes: as many blocks as are resident at once
   int nsm = 0, by = 0, bz = 0;
   BSK_CHECK_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const size_t z_smem = (2 * (size_t)kZLines * (N + 1) + N) * sizeof(float2);
+  size_t z_smem = (2 * (size_t)kZLines * (N + 1) + N) * sizeof(float2);
+  if constexpr (NC != 0) z_smem += z_twl_size<NC>() * sizeof(float2);
   BSK_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by, synth_y_kernel<NC>, kThreads,
                                                                fft_smem));
   BSK_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bz, synth_z_kernel<NC>, kThreads,
