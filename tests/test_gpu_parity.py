@@ -171,6 +171,26 @@ def test_fields_match_oracle_grid_level_sizes(cuda, n):
     plan.close()
 
 
+def test_fields_match_oracle_480(cuda):
+    # the 1024^3 workload's reduced grid (16x6x5 plan, radix-5 last pass over 96 butterflies a
+    # line); three shells out to radius 181, beyond the Z pass's register prefetch (128 q_c)
+    n, box, edges, _ = _small(480, 100.0, 60, 0.45)
+    assert len(edges) == 3
+    delta = synthetic.lognormal_mesh_torch(n, box, seed=19, device=cuda).contiguous()
+    plan = Plan(n, box, edges, grid="native")
+    plan.paint(0, delta)
+    got = [plan.field(0, s).cpu().numpy() for s in range(len(edges))]
+    plan.sync_check()
+    plan.close()
+    host = delta.cpu().numpy()
+    del delta
+    torch.cuda.empty_cache()
+    of = O.shell_fields(O.spectrum(host), n, box, edges)
+    for s in range(len(edges)):
+        scale = np.abs(of[s]).max()
+        assert np.abs(got[s].astype(np.float64) - of[s]).max() <= 1e-5 * scale, s
+
+
 def test_paint_keeps_input(cuda):
     n, box, edges, _ = _small(32, 100.0, 2)
     delta = torch.from_numpy(synthetic.lognormal_mesh(n, box, seed=12)).cuda()
