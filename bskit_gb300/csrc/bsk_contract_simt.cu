@@ -1,4 +1,4 @@
-// SIMT triple-product contraction: the plain-FP32 path and the FP64 GPU oracle.
+// SIMT triple-product contraction: the plain-FP32 path and the FP64 yardstick.
 //
 // The FP64 variants (FP32 or FP64 fields, FP64 products and sums):
 // Work item = (sub-tile of 128 pair rows x 32 third-shell columns, K slice).
@@ -368,7 +368,7 @@ void launch_contract_simt_f32(const DeviceSchedule& s, const float* f1, const fl
   BSK_CHECK_CUDA(cudaGetLastError());
 }
 
-// FP64 products and sums of FP32 fields (the GPU oracle of the precision study).
+// FP64 products and sums of FP32 fields (the yardstick of the precision study).
 void launch_contract_simt_f64(const DeviceSchedule& s, const float* f1, const float* f2,
                               const float* f3, int n_shells, int64_t K, int64_t k_begin,
                               int64_t k_end, double* out, int num_sms, cudaStream_t st,

@@ -53,7 +53,7 @@ enum bsk_status {
 
 /* Arithmetic of the triple-product contraction. */
 enum bsk_precision {
-  BSK_PREC_FP64 = 0,    /* FP64 SIMT on the FP32 shell fields (GPU oracle)              */
+  BSK_PREC_FP64 = 0,    /* FP64 SIMT on the FP32 shell fields (the FP64 yardstick)      */
   BSK_PREC_FP32 = 1,    /* plain FP32 SIMT, FP64 cross-slice sum                        */
   BSK_PREC_BF16X3 = 2,  /* tcgen05 bf16 hi*hi + hi*lo + lo*hi, FP32 accumulate, FP64 sum */
   BSK_PREC_BF16 = 3     /* tcgen05 bf16 hi*hi only                                      */
